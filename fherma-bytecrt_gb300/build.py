@@ -1,0 +1,87 @@
+"""Build recipe for the in-tree native libraries (sm_103a only).
+
+    python -c "import importlib; importlib.import_module('fherma-bytecrt_gb300.build').build()"
+
+Compiles csrc/*.cu with nvcc for sm_103a, in parallel, into
+libbytecrt_gb300.so (the C ABI of include/bytecrt_gb300.h) and
+libfherma_gb300.so (the reference's C++ plugin ABI on top of it), plus the
+`solution` harness binary.  Objects go to _build/ (git-ignored).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(REPO, "_build")
+LIB = os.path.join(HERE, "libbytecrt_gb300.so")
+SHIM = os.path.join(HERE, "libfherma_gb300.so")
+HARNESS = os.path.join(HERE, "solution")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CORE_SOURCES = ["plan.cu", "encode.cu", "ntt.cu", "crt.cu", "engine.cu", "capi.cu"]
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return path
+
+
+def _flags():
+    return ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-O3,-fopenmp",
+            "-I", os.path.join(REPO, "include")]
+
+
+def _headers():
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".hpp", ".cuh", ".h"))] + \
+        [os.path.join(REPO, "include", f) for f in os.listdir(os.path.join(REPO, "include"))]
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _compile(src: str) -> str:
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    if _stale(obj, [src, *_headers(), __file__]):
+        cmd = [nvcc(), *_flags(), "-c", src, "-o", obj + ".tmp"]
+        subprocess.run(cmd, check=True)
+        os.replace(obj + ".tmp", obj)
+    return obj
+
+
+def build(verbose: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    sources = [os.path.join(CSRC, s) for s in CORE_SOURCES]
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(_compile, sources))
+    if _stale(LIB, objs):
+        tmp = LIB + f".tmp{os.getpid()}"
+        subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fopenmp", "-lgomp"],
+                       check=True)
+        os.replace(tmp, LIB)
+    shim_src = os.path.join(CSRC, "fherma_shim.cpp")
+    if os.path.exists(shim_src) and _stale(SHIM, [shim_src, LIB, *_headers()]):
+        tmp = SHIM + f".tmp{os.getpid()}"
+        subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", os.path.join(REPO, "include"),
+                        "-o", tmp, shim_src, "-L", HERE, "-lbytecrt_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
+        os.replace(tmp, SHIM)
+    harness_src = os.path.join(CSRC, "harness.cpp")
+    if os.path.exists(harness_src) and os.path.exists(SHIM) and _stale(HARNESS, [harness_src, SHIM]):
+        tmp = HARNESS + f".tmp{os.getpid()}"
+        subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(REPO, "include"), "-o", tmp,
+                        harness_src, "-L", HERE, "-lfherma_gb300", "-lbytecrt_gb300",
+                        "-Wl,-rpath,$ORIGIN"], check=True)
+        os.replace(tmp, HARNESS)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build())

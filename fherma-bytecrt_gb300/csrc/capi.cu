@@ -1,0 +1,186 @@
+// extern "C" boundary (include/bytecrt_gb300.h): status codes in, exceptions
+// never cross it.  The reference converts every CUDA error into a C++
+// exception at the plugin boundary (native-smoke/solve.cu:46-49); here the C
+// ABI returns a code and the C++ plugin shim turns it back into an exception.
+#include "../../include/bytecrt_gb300.h"
+#include "engine.hpp"
+
+#include <cstring>
+#include <new>
+
+struct bcg_plan {
+    bcg::HostPlan plan;
+};
+struct bcg_context {
+    std::unique_ptr<bcg::Context> ctx;
+};
+
+namespace {
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return BCG_OK;
+    } catch (const std::invalid_argument& e) {
+        bcg::set_last_error(e.what());
+        return BCG_ERR_INVALID;
+    } catch (const bcg::DeviceTimeout& e) {
+        bcg::set_last_error(e.what());
+        return BCG_ERR_DEVICE_TIMEOUT;
+    } catch (const bcg::CudaError& e) {
+        bcg::set_last_error(e.what());
+        return (e.code == cudaErrorMemoryAllocation) ? BCG_ERR_NOMEM : BCG_ERR_CUDA;
+    } catch (const std::bad_alloc& e) {
+        bcg::set_last_error("host allocation failed");
+        return BCG_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        bcg::set_last_error(e.what());
+        return BCG_ERR_INVALID;
+    }
+}
+
+void fill_info(const bcg::HostPlan& p, bcg_info* out, uint32_t group) {
+    const bcg::Geometry& g = p.g;
+    std::memset(out, 0, sizeof *out);
+    out->N = g.N; out->W = g.W; out->L = g.L; out->P = g.P; out->kpad = g.kpad;
+    out->enc_k = g.enc_k; out->enc_cols = g.enc_cols; out->crt_k = g.crt_k_total; out->crt_n = g.crt_n;
+    out->product_bits = g.product_bits;
+    out->group = group;
+    out->workspace_bytes_per_product = uint64_t(2) * g.P * g.N * 4;
+}
+
+void require(bool ok, const char* what) {
+    if (!ok) throw std::invalid_argument(what);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bcg_last_error(void) { return bcg::last_error(); }
+
+int bcg_plan_create(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, bcg_plan** out) {
+    return guarded([&] {
+        require(q && out, "null argument");
+        *out = nullptr;
+        auto* p = new bcg_plan{bcg::make_plan(N, W, L, q)};
+        *out = p;
+    });
+}
+
+void bcg_plan_destroy(bcg_plan* plan) { delete plan; }
+
+int bcg_plan_info(const bcg_plan* plan, bcg_info* out) {
+    return guarded([&] {
+        require(plan && out, "null argument");
+        fill_info(plan->plan, out, 0);
+    });
+}
+
+int bcg_plan_primes(const bcg_plan* plan, uint32_t* primes, uint32_t* psi, uint32_t* crt_inverse) {
+    return guarded([&] {
+        require(plan, "null argument");
+        const auto& p = plan->plan;
+        if (primes) std::memcpy(primes, p.primes.data(), p.primes.size() * 4);
+        if (psi) std::memcpy(psi, p.psi.data(), p.psi.size() * 4);
+        if (crt_inverse) std::memcpy(crt_inverse, p.crt_inverse.data(), p.crt_inverse.size() * 4);
+    });
+}
+
+int bcg_plan_weights(const bcg_plan* plan, uint32_t* weights) {
+    return guarded([&] {
+        require(plan && weights, "null argument");
+        std::memcpy(weights, plan->plan.weights.data(), plan->plan.weights.size() * 4);
+    });
+}
+
+int bcg_context_create(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int device, bcg_context** out) {
+    return guarded([&] {
+        require(q && out, "null argument");
+        *out = nullptr;
+        auto c = std::make_unique<bcg_context>();
+        c->ctx = std::make_unique<bcg::Context>(N, W, L, q, device);
+        *out = c.release();
+    });
+}
+
+void bcg_context_destroy(bcg_context* ctx) { delete ctx; }
+
+int bcg_context_info(const bcg_context* ctx, bcg_info* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        fill_info(ctx->ctx->plan(), out, ctx->ctx->group());
+    });
+}
+
+int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count) {
+    return guarded([&] {
+        require(ctx, "null context");
+        if (count == 0) return;
+        require(a && b && c, "null buffer");
+        ctx->ctx->multiply_host(a, b, c, count);
+    });
+}
+
+int bcg_multiply_device(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count,
+                        void* stream) {
+    return guarded([&] {
+        require(ctx, "null context");
+        if (count == 0) return;
+        require(a && b && c, "null buffer");
+        ctx->ctx->multiply_device(a, b, c, count, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int bcg_encode_device(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* planes_a,
+                      uint32_t* planes_b, size_t plane_stride, uint32_t count, void* stream) {
+    return guarded([&] {
+        require(ctx && a && b && planes_a && planes_b, "null argument");
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->ctx->stream();
+        ctx->ctx->encode(a, b, planes_a, planes_b, plane_stride, count, st);
+    });
+}
+
+int bcg_negacyclic_device(bcg_context* ctx, uint32_t* planes_a, uint32_t* planes_b, size_t plane_stride,
+                          uint32_t count, void* stream) {
+    return guarded([&] {
+        require(ctx && planes_a && planes_b, "null argument");
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->ctx->stream();
+        ctx->ctx->negacyclic(planes_a, planes_b, plane_stride, count, st);
+    });
+}
+
+int bcg_crt_device(bcg_context* ctx, const uint32_t* terms, size_t plane_stride, uint32_t* c, uint32_t count,
+                   void* stream) {
+    return guarded([&] {
+        require(ctx && terms && c, "null argument");
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->ctx->stream();
+        ctx->ctx->crt(terms, plane_stride, c, count, st);
+    });
+}
+
+int bcg_synchronize(bcg_context* ctx) {
+    return guarded([&] {
+        require(ctx, "null context");
+        bcg::check(cudaDeviceSynchronize(), "device synchronize");
+        ctx->ctx->check_status();
+    });
+}
+
+int bcg_profile_enable(bcg_context* ctx, int enable) {
+    return guarded([&] {
+        require(ctx, "null context");
+        ctx->ctx->set_profiling(enable != 0);
+    });
+}
+
+int bcg_profile_read(bcg_context* ctx, bcg_profile* out, int reset) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        std::memset(out, 0, sizeof *out);
+        ctx->ctx->read_profile(out->ms, out->launches, &out->chains, reset != 0);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,316 @@
+// Host engine: device tables, workspace and the launch chain (see engine.hpp).
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <omp.h>
+
+namespace bcg {
+
+namespace {
+thread_local std::string g_last_error;
+
+// Parallel host copy for the pinned staging of host-buffer calls (the
+// reference packs operands with up to 12 OpenMP workers, native-smoke/io-copy.cpp:29-42).
+void parallel_copy(void* dst, const void* src, size_t bytes) {
+    if (bytes < (size_t(1) << 20)) { std::memcpy(dst, src, bytes); return; }
+    const int workers = std::min(16, omp_get_num_procs());
+    const size_t chunk = (bytes + workers - 1) / workers;
+#pragma omp parallel for num_threads(workers) schedule(static)
+    for (int t = 0; t < workers; ++t) {
+        const size_t begin = size_t(t) * chunk;
+        if (begin < bytes)
+            std::memcpy(static_cast<char*>(dst) + begin, static_cast<const char*>(src) + begin,
+                        std::min(chunk, bytes - begin));
+    }
+}
+}  // namespace
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error() { return g_last_error.c_str(); }
+
+Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int device)
+    : plan_(make_plan(N, W, L, q)), device_(device) {
+    check(cudaSetDevice(device_), "select device");
+    const Geometry& g = plan_.g;
+    check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+    check(cudaStreamCreateWithFlags(&copy_in_, cudaStreamNonBlocking), "stream");
+    check(cudaStreamCreateWithFlags(&copy_out_, cudaStreamNonBlocking), "stream");
+    for (int s = 0; s < 2; ++s) {
+        check(cudaEventCreateWithFlags(&ev_in_[s], cudaEventDisableTiming), "event");
+        check(cudaEventCreateWithFlags(&ev_done_[s], cudaEventDisableTiming), "event");
+        check(cudaEventCreateWithFlags(&ev_out_[s], cudaEventDisableTiming), "event");
+    }
+    auto upload = [&](DeviceBuffer& buf, const void* src, size_t bytes) {
+        buf.allocate(bytes);
+        check(cudaMemcpy(buf.ptr, src, bytes, cudaMemcpyHostToDevice), "table upload");
+    };
+    upload(consts_, plan_.prime_consts.data(), plan_.prime_consts.size() * 4);
+    upload(tables_, plan_.ntt_tables.data(), plan_.ntt_tables.size() * 4);
+    upload(enc_b_, plan_.enc_b.data(), plan_.enc_b.size() * 2);
+    upload(crt_b_, plan_.crt_b.data(), plan_.crt_b.size() * 2);
+    upload(invp_, plan_.invp.data(), plan_.invp.size() * 4);
+    upload(q_, plan_.q.data(), plan_.q.size() * 4);
+    status_.allocate(16);
+    check(cudaMemset(status_.ptr, 0, 16), "status reset");
+
+    const TableOffsets off = table_offsets(g);
+    ntt_.consts = consts_.as<uint4>();
+    ntt_.tables = tables_.as<uint2>();
+    ntt_.table_stride = g.table_stride;
+    ntt_.off_col_f = off.col_f; ntt_.off_col_i = off.col_i;
+    ntt_.off_row_f = off.row_f; ntt_.off_row_i = off.row_i;
+    ntt_.off_tw_lo = off.tw_lo; ntt_.off_tw_hi = off.tw_hi;
+    ntt_.off_itw_lo = off.itw_lo; ntt_.off_itw_hi = off.itw_hi;
+    ntt_.N = g.N; ntt_.P = g.P; ntt_.c_bits = g.c_bits; ntt_.z_bits = g.z_bits; ntt_.Z = g.Z; ntt_.H = g.H;
+
+    enc_.enc_b = enc_b_.as<uint16_t>();
+    enc_.consts = consts_.as<uint4>();
+    enc_.N = g.N; enc_.L = g.L; enc_.P = g.P; enc_.K = g.enc_k; enc_.cols = g.enc_cols; enc_.chunks = g.enc_chunks;
+    enc_.status = status_.as<uint32_t>();
+
+    crt_.crt_b = crt_b_.as<uint16_t>();
+    crt_.invp = invp_.as<float>();
+    crt_.q = q_.as<uint32_t>();
+    crt_.q_inv_scaled = plan_.q_inv_scaled;
+    crt_.N = g.N; crt_.L = g.L; crt_.P = g.P; crt_.k_total = g.crt_k_total; crt_.kchunks = g.crt_kchunks;
+    crt_.E = g.crt_e; crt_.NC = g.crt_n;
+    crt_.status = status_.as<uint32_t>();
+
+    group_ = std::max<uint32_t>(1, 65536 / g.N);
+}
+
+Context::~Context() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (const Mark& m : marks_) { cudaEventDestroy(m.begin); cudaEventDestroy(m.end); }
+    for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
+    for (int s = 0; s < 2; ++s) {
+        if (ev_in_[s]) cudaEventDestroy(ev_in_[s]);
+        if (ev_done_[s]) cudaEventDestroy(ev_done_[s]);
+        if (ev_out_[s]) cudaEventDestroy(ev_out_[s]);
+    }
+    if (copy_in_) cudaStreamDestroy(copy_in_);
+    if (copy_out_) cudaStreamDestroy(copy_out_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Context::set_group(uint32_t g) { group_ = std::max<uint32_t>(1, g); }
+
+void Context::ensure_workspace(uint32_t products) {
+    if (products <= ws_products_) return;
+    cudaStreamSynchronize(stream_);
+    ws_.allocate(size_t(products) * workspace_bytes_per_product());
+    ws_products_ = products;
+}
+
+void Context::ensure_host_staging(uint32_t products) {
+    if (products <= io_products_) return;
+    cudaStreamSynchronize(stream_);
+    cudaStreamSynchronize(copy_in_);
+    cudaStreamSynchronize(copy_out_);
+    const size_t bytes = size_t(products) * coeff_words() * 4 * 3;
+    for (int s = 0; s < 2; ++s) {
+        io_dev_[s].allocate(bytes);
+        io_host_[s].allocate(bytes);
+    }
+    io_products_ = products;
+}
+
+void Context::encode(const uint32_t* a, const uint32_t* b, uint32_t* pa, uint32_t* pb, size_t plane_stride,
+                     uint32_t count, cudaStream_t st) {
+    EncodeArgs e = enc_;
+    e.in0 = a; e.in1 = b; e.in_stride = coeff_words();
+    e.out0 = pa; e.out1 = pb; e.out_stride = plane_stride;
+    check(launch_encode(e, count, st), "encode launch");
+}
+
+void Context::negacyclic(uint32_t* pa, uint32_t* pb, size_t plane_stride, uint32_t count, cudaStream_t st) {
+    check(launch_col_forward(ntt_, pa, plane_stride, count, st), "column pass launch");
+    check(launch_col_forward(ntt_, pb, plane_stride, count, st), "column pass launch");
+    check(launch_row_product(ntt_, pa, plane_stride, pb, plane_stride, pa, plane_stride, count, false, st),
+          "row pass launch");
+    check(launch_col_inverse(ntt_, pa, plane_stride, count, st), "inverse column pass launch");
+}
+
+void Context::crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint32_t count, cudaStream_t st) {
+    CrtArgs a = crt_;
+    a.terms = terms; a.terms_stride = plane_stride;
+    a.out = c; a.out_stride = coeff_words();
+    check(launch_crt(a, count, st), "CRT launch");
+}
+
+void Context::mark_begin(int stage, cudaStream_t st) {
+    ++stage_launches_[stage];
+    ++launches_total_;
+    if (!profiling_) return;
+    auto take = [&]() {
+        if (event_pool_.empty()) {
+            cudaEvent_t e;
+            check(cudaEventCreate(&e), "profile event");
+            return e;
+        }
+        cudaEvent_t e = event_pool_.back();
+        event_pool_.pop_back();
+        return e;
+    };
+    Mark m{stage, take(), take()};
+    check(cudaEventRecord(m.begin, st), "profile event");
+    marks_.push_back(m);
+}
+
+void Context::mark_end(cudaStream_t st) {
+    if (!profiling_ || marks_.empty()) return;
+    check(cudaEventRecord(marks_.back().end, st), "profile event");
+}
+
+void Context::read_profile(double* ms, uint64_t* launches, uint64_t* chains, bool reset) {
+    for (int s = 0; s < kStages; ++s) ms[s] = 0;
+    for (const Mark& m : marks_) {
+        check(cudaEventSynchronize(m.end), "profile event");
+        float t = 0;
+        check(cudaEventElapsedTime(&t, m.begin, m.end), "profile elapsed");
+        ms[m.stage] += t;
+    }
+    for (int s = 0; s < kStages; ++s) launches[s] = stage_launches_[s];
+    *chains = chains_;
+    if (reset) {
+        for (const Mark& m : marks_) { event_pool_.push_back(m.begin); event_pool_.push_back(m.end); }
+        marks_.clear();
+        for (auto& l : stage_launches_) l = 0;
+        chains_ = 0;
+    }
+}
+
+void Context::chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, uint32_t* ws,
+                    cudaStream_t st) {
+    // Workspace per product: [A planes | B planes]; the product overwrites A.
+    const size_t pw = plane_words();
+    uint32_t* pa = ws;
+    uint32_t* pb = ws + pw;
+    const size_t stride = 2 * pw;
+    ++chains_;
+    mark_begin(kEncode, st);
+    encode(a, b, pa, pb, stride, count, st);
+    mark_end(st);
+    // Both operands' column passes in one launch (sets alternate A, B).
+    if (geom().C > 1) {
+        mark_begin(kColForward, st);
+        check(launch_col_forward(ntt_, pa, pw, 2 * count, st), "column pass launch");
+        mark_end(st);
+    }
+    mark_begin(kRow, st);
+    check(launch_row_product(ntt_, pa, stride, pb, stride, pa, stride, count, false, st), "row pass launch");
+    mark_end(st);
+    if (geom().C > 1) {
+        mark_begin(kColInverse, st);
+        check(launch_col_inverse(ntt_, pa, stride, count, st), "inverse column pass launch");
+        mark_end(st);
+    }
+    mark_begin(kCrt, st);
+    crt(pa, stride, c, count, st);
+    mark_end(st);
+}
+
+void Context::forward_spectral(const uint32_t* x, uint32_t* planes, cudaStream_t st) {
+    EncodeArgs e = enc_;
+    e.in0 = x; e.in1 = x; e.in_stride = 0;
+    e.out0 = planes; e.out1 = planes; e.out_stride = 0;
+    check(launch_encode(e, 1, st, 1), "encode launch");
+    check(launch_col_forward(ntt_, planes, 0, 1, st), "column pass launch");
+    check(launch_row_forward(ntt_, planes, 0, 1, st), "row forward launch");
+}
+
+void Context::multiply_spectral_device(const uint32_t* a_spectral, const uint32_t* b, uint32_t* c,
+                                       uint32_t count, uint32_t* ws, cudaStream_t st) {
+    const size_t pw = plane_words();
+    EncodeArgs e = enc_;
+    e.in0 = b; e.in1 = b; e.in_stride = coeff_words();
+    e.out0 = ws; e.out1 = ws; e.out_stride = pw;
+    check(launch_encode(e, count, st, 1), "encode launch");
+    check(launch_col_forward(ntt_, ws, pw, count, st), "column pass launch");
+    check(launch_row_product(ntt_, a_spectral, 0, ws, pw, ws, pw, count, true, st), "row pass launch");
+    check(launch_col_inverse(ntt_, ws, pw, count, st), "inverse column pass launch");
+    crt(ws, pw, c, count, st);
+}
+
+void Context::multiply_device(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count,
+                              cudaStream_t st) {
+    if (!st) st = stream_;
+    const uint32_t g = std::min(group_, std::max<uint32_t>(count, 1));
+    ensure_workspace(g);
+    const size_t cw = coeff_words();
+    for (uint32_t done = 0; done < count; done += g) {
+        const uint32_t n = std::min(g, count - done);
+        chain(a + done * cw, b + done * cw, c + done * cw, n, ws_.as<uint32_t>(), st);
+    }
+}
+
+namespace {
+bool is_pinned(const void* p) {
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeHost;
+}
+}  // namespace
+
+void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count) {
+    if (count == 0) return;
+    if (is_pinned(a) && is_pinned(b) && is_pinned(c)) {
+        multiply_pinned(a, b, c, count);
+        return;
+    }
+    const uint32_t g = std::min(group_, count);
+    ensure_workspace(g);
+    ensure_host_staging(g);
+    const size_t cw = coeff_words();
+    const uint32_t ngroups = (count + g - 1) / g;
+    auto group_size = [&](uint32_t gi) { return std::min(g, count - gi * g); };
+    auto drain = [&](uint32_t gi) {
+        const int s = gi & 1;
+        check(cudaEventSynchronize(ev_out_[s]), "output copy");
+        const size_t words = size_t(group_size(gi)) * cw;
+        parallel_copy(c + size_t(gi) * g * cw, io_host_[s].as<uint32_t>() + 2 * g * cw, words * 4);
+    };
+    for (uint32_t gi = 0; gi < ngroups; ++gi) {
+        const int s = gi & 1;
+        if (gi >= 2) drain(gi - 2);
+        const uint32_t n = group_size(gi);
+        const size_t words = size_t(n) * cw;
+        uint32_t* h = io_host_[s].as<uint32_t>();
+        uint32_t* d = io_dev_[s].as<uint32_t>();
+        parallel_copy(h, a + size_t(gi) * g * cw, words * 4);
+        parallel_copy(h + g * cw, b + size_t(gi) * g * cw, words * 4);
+        if (gi >= 2) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
+        check(cudaMemcpyAsync(d, h, words * 4, cudaMemcpyHostToDevice, copy_in_), "input copy");
+        check(cudaMemcpyAsync(d + g * cw, h + g * cw, words * 4, cudaMemcpyHostToDevice, copy_in_), "input copy");
+        check(cudaEventRecord(ev_in_[s], copy_in_), "event");
+        check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
+        chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_);
+        check(cudaEventRecord(ev_done_[s], stream_), "event");
+        check(cudaStreamWaitEvent(copy_out_, ev_done_[s], 0), "event wait");
+        check(cudaMemcpyAsync(h + 2 * g * cw, d + 2 * g * cw, words * 4, cudaMemcpyDeviceToHost, copy_out_),
+              "output copy");
+        check(cudaEventRecord(ev_out_[s], copy_out_), "event");
+    }
+    for (uint32_t gi = ngroups >= 2 ? ngroups - 2 : 0; gi < ngroups; ++gi) drain(gi);
+    check_status();
+}
+
+void Context::check_status() {
+    uint32_t st = 0;
+    check(cudaMemcpy(&st, status_.ptr, 4, cudaMemcpyDeviceToHost), "status read");
+    if (st != kStatusOk) {
+        check(cudaMemset(status_.ptr, 0, 4), "status reset");
+        throw DeviceTimeout("a kernel's bounded wait ran out (device status " + std::to_string(st) + ")");
+    }
+}
+
+void Context::synchronize(cudaStream_t st) {
+    check(cudaStreamSynchronize(st ? st : stream_), "stream synchronize");
+    check_status();
+}
+
+}  // namespace bcg

@@ -1,0 +1,148 @@
+// Host engine: one Context per point (N, W, q) on one GPU.  It owns the
+// device copies of the plan tables, a plane workspace for `group` products,
+// pinned staging for host-buffer calls, and the launch chain
+//   encode -> column pass (A,B) -> row pass (product) -> inverse column pass -> CRT.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "kernels.hpp"
+#include "ntt.cuh"
+#include "plan.hpp"
+
+namespace bcg {
+
+class CudaError : public std::runtime_error {
+public:
+    CudaError(const std::string& what, cudaError_t e)
+        : std::runtime_error(what + ": " + cudaGetErrorString(e)), code(e) {}
+    cudaError_t code;
+};
+
+class DeviceTimeout : public std::runtime_error {
+public:
+    using std::runtime_error::runtime_error;
+};
+
+inline void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(what, e);
+}
+
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    ~DeviceBuffer() { if (ptr) cudaFree(ptr); }
+    void allocate(size_t n) {
+        if (ptr) { cudaFree(ptr); ptr = nullptr; bytes = 0; }
+        if (n) { check(cudaMalloc(&ptr, n), "device allocation"); bytes = n; }
+    }
+    template <class T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+struct PinnedBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    PinnedBuffer() = default;
+    PinnedBuffer(const PinnedBuffer&) = delete;
+    PinnedBuffer& operator=(const PinnedBuffer&) = delete;
+    ~PinnedBuffer() { if (ptr) cudaFreeHost(ptr); }
+    void allocate(size_t n) {
+        if (ptr) { cudaFreeHost(ptr); ptr = nullptr; bytes = 0; }
+        if (n) { check(cudaMallocHost(&ptr, n), "pinned allocation"); bytes = n; }
+    }
+    template <class T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+class Context {
+public:
+    Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int device);
+    ~Context();
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+
+    const HostPlan& plan() const { return plan_; }
+    const Geometry& geom() const { return plan_.g; }
+    int device() const { return device_; }
+    cudaStream_t stream() const { return stream_; }
+    uint32_t group() const { return group_; }
+    void set_group(uint32_t g);
+    size_t plane_words() const { return size_t(plan_.g.P) * plan_.g.N; }
+    size_t coeff_words() const { return size_t(plan_.g.N) * plan_.g.L; }
+    size_t workspace_bytes_per_product() const { return 2 * plane_words() * sizeof(uint32_t); }
+
+    // Stages (device pointers, asynchronous on st).
+    void encode(const uint32_t* a, const uint32_t* b, uint32_t* pa, uint32_t* pb, size_t plane_stride,
+                uint32_t count, cudaStream_t st);
+    void negacyclic(uint32_t* pa, uint32_t* pb, size_t plane_stride, uint32_t count, cudaStream_t st);
+    void crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint32_t count, cudaStream_t st);
+    // Spectral form of an operand: encode + column pass + forward row pass.
+    void forward_spectral(const uint32_t* x, uint32_t* planes, cudaStream_t st);
+    // c = a * b where a is given in spectral form (planes, shared by all count products).
+    void multiply_spectral_device(const uint32_t* a_spectral, const uint32_t* b, uint32_t* c, uint32_t count,
+                                  uint32_t* workspace, cudaStream_t st);
+
+    // Whole products.
+    void multiply_device(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, cudaStream_t st);
+    void multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
+
+    // Throws DeviceTimeout (after clearing it) if a kernel reported a wait timeout.
+    void synchronize(cudaStream_t st);
+    void check_status();
+
+    // One product chain on a caller-provided workspace of >= count products.
+    void chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, uint32_t* ws, cudaStream_t st);
+
+    NttArgs ntt_args() const { return ntt_; }
+
+    // Per-stage timing with CUDA events recorded on the launching stream.
+    enum Stage { kEncode = 0, kColForward, kRow, kColInverse, kCrt, kStages };
+    void set_profiling(bool on) { profiling_ = on; }
+    // Sums the elapsed time of every recorded stage (synchronizes on them).
+    void read_profile(double* ms, uint64_t* launches, uint64_t* chains, bool reset);
+    uint64_t launches() const { return launches_total_; }
+
+private:
+    struct Mark { int stage; cudaEvent_t begin, end; };
+    void mark_begin(int stage, cudaStream_t st);
+    void mark_end(cudaStream_t st);
+    bool profiling_ = false;
+    std::vector<Mark> marks_;
+    std::vector<cudaEvent_t> event_pool_;
+    uint64_t stage_launches_[kStages] = {};
+    uint64_t launches_total_ = 0, chains_ = 0;
+
+    void ensure_workspace(uint32_t products);
+    void ensure_host_staging(uint32_t products);
+
+    HostPlan plan_;
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+    cudaStream_t copy_in_ = nullptr, copy_out_ = nullptr;
+    uint32_t group_ = 1;
+    DeviceBuffer consts_, tables_, enc_b_, crt_b_, invp_, q_, status_;
+    DeviceBuffer ws_;
+    size_t ws_products_ = 0;
+    // Host-buffer path: double-buffered device inputs/outputs and pinned staging.
+    DeviceBuffer io_dev_[2];
+    PinnedBuffer io_host_[2];
+    size_t io_products_ = 0;
+    cudaEvent_t ev_in_[2] = {}, ev_done_[2] = {}, ev_out_[2] = {};
+    NttArgs ntt_{};
+    EncodeArgs enc_{};
+    CrtArgs crt_{};
+};
+
+// Thread-local last error message for the C ABI.
+void set_last_error(const std::string& msg);
+const char* last_error();
+
+}  // namespace bcg

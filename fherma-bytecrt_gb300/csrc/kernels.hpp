@@ -1,0 +1,56 @@
+// Launch interfaces of the sm_103a kernels (host side of csrc/*.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "plan.hpp"
+
+namespace bcg {
+
+struct EncodeArgs {
+    const uint32_t* in0;     // operand A coefficients [N][L] (product z at + z*in_stride)
+    const uint32_t* in1;     // operand B
+    size_t in_stride;
+    uint32_t* out0;          // residue planes [P][N] of A (product z at + z*out_stride)
+    uint32_t* out1;
+    size_t out_stride;
+    const uint16_t* enc_b;   // fp16 byte-power matrix, chunked
+    const uint4* consts;     // per prime: p, p^-1, -p^-1, 0
+    uint32_t N, L, P, K, cols, chunks;
+    uint32_t* status;
+};
+
+struct CrtArgs {
+    const uint32_t* terms;   // t_j planes [P][N] (product z at + z*terms_stride)
+    size_t terms_stride;
+    uint32_t* out;           // [N][L] canonical limbs
+    size_t out_stride;
+    const uint16_t* crt_b;   // fp16 weight-digit matrix, chunked over K
+    const float* invp;
+    const uint32_t* q;
+    double q_inv_scaled;
+    uint32_t N, L, P, k_total, kchunks, E, NC;
+    uint32_t* status;
+};
+
+struct NttArgs;   // ntt.cuh
+
+size_t encode_smem_bytes(uint32_t K);
+size_t crt_smem_bytes(uint32_t NC);
+
+// Encodes operand A (and operand B when operands == 2) of nprod products (grid.y = operand).
+cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands = 2);
+cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st);
+
+// Column passes over nplanes prime-plane sets, set z at planes + z*stride.
+cudaError_t launch_col_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st);
+cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st);
+cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_t a_stride,
+                               const uint32_t* planes_b, size_t b_stride, uint32_t* planes_out,
+                               size_t out_stride, uint32_t nprod, bool a_spectral, cudaStream_t st);
+cudaError_t launch_row_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st);
+size_t row_smem_bytes(const NttArgs& a, bool forward_only);
+
+}  // namespace bcg

@@ -1,0 +1,336 @@
+// NTT kernels (see ntt.cuh for the decomposition).
+#include "ntt.cuh"
+#include "kernels.hpp"
+
+namespace bcg {
+namespace {
+
+__host__ __device__ constexpr int local_bits(int bits) { return bits < 3 ? bits : 3; }
+
+// ------------------------------------------------------------ column pass --
+// One CTA: 32 adjacent columns (lane = column) of one plane and one prime.
+// Each thread keeps 8 elements of its column in registers per phase of three
+// levels; between phases the tile goes through shared memory, one 128-byte
+// row per warp access (conflict free).
+template <int CB, bool INVERSE, int PH>
+__device__ __forceinline__ void col_phase(uint32_t (&x)[1 << local_bits(CB)], uint32_t w, uint32_t p,
+                                          const uint2* __restrict__ tw) {
+    constexpr int LOCAL = local_bits(CB);
+    constexpr PhaseMap<CB, LOCAL> map(PH);
+    auto twiddle = [&](int level, uint32_t s) { return __ldg(tw + (1u << level) + (s >> (CB - level))); };
+    if constexpr (INVERSE) phase_gs<CB, LOCAL>(x, map, w, p, twiddle);
+    else phase_ct<CB, LOCAL>(x, map, w, p, twiddle);
+}
+
+template <int CB, int FROM, int TO>
+__device__ __forceinline__ void col_exchange(uint32_t (&x)[1 << local_bits(CB)], uint32_t* buf,
+                                             uint32_t w, uint32_t lane) {
+    constexpr int LOCAL = local_bits(CB);
+    constexpr PhaseMap<CB, LOCAL> from(FROM), to(TO);
+#pragma unroll
+    for (uint32_t k = 0; k < (1u << LOCAL); ++k) buf[from.index(w, k) * 32 + lane] = x[k];
+    __syncthreads();
+#pragma unroll
+    for (uint32_t k = 0; k < (1u << LOCAL); ++k) x[k] = buf[to.index(w, k) * 32 + lane];
+    __syncthreads();
+}
+
+template <int CB, bool INVERSE>
+__global__ void __launch_bounds__(32 * ((1 << CB) >> local_bits(CB)))
+col_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride) {
+    constexpr int LOCAL = local_bits(CB);
+    constexpr int NPH = phase_count(CB);
+    constexpr uint32_t R = 256;
+    __shared__ uint32_t buf[(1 << CB) * 32];
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t j = blockIdx.y;
+    const uint32_t p = a.consts[j].x;
+    uint32_t* col = planes + size_t(blockIdx.z) * plane_stride + size_t(j) * a.N + blockIdx.x * 32 + lane;
+    const uint2* tw = a.tables + size_t(j) * a.table_stride + (INVERSE ? a.off_col_i : a.off_col_f);
+    uint32_t x[1 << LOCAL];
+    constexpr int first = INVERSE ? NPH - 1 : 0;
+    constexpr int last = INVERSE ? 0 : NPH - 1;
+    {
+        constexpr PhaseMap<CB, LOCAL> m(first);
+#pragma unroll
+        for (uint32_t k = 0; k < (1u << LOCAL); ++k) x[k] = col[size_t(m.index(w, k)) * R];
+    }
+    if constexpr (!INVERSE) {
+        col_phase<CB, false, 0>(x, w, p, tw);
+        if constexpr (NPH > 1) { col_exchange<CB, 0, 1>(x, buf, w, lane); col_phase<CB, false, 1>(x, w, p, tw); }
+        if constexpr (NPH > 2) { col_exchange<CB, 1, 2>(x, buf, w, lane); col_phase<CB, false, 2>(x, w, p, tw); }
+    } else {
+        if constexpr (NPH > 2) { col_phase<CB, true, 2>(x, w, p, tw); col_exchange<CB, 2, 1>(x, buf, w, lane); }
+        if constexpr (NPH > 1) { col_phase<CB, true, 1>(x, w, p, tw); col_exchange<CB, 1, 0>(x, buf, w, lane); }
+        col_phase<CB, true, 0>(x, w, p, tw);
+#pragma unroll
+        for (uint32_t k = 0; k < (1u << LOCAL); ++k) x[k] = reduce_once(x[k], p);
+    }
+    {
+        constexpr PhaseMap<CB, LOCAL> m(last);
+#pragma unroll
+        for (uint32_t k = 0; k < (1u << LOCAL); ++k) col[size_t(m.index(w, k)) * R] = x[k];
+    }
+}
+
+// --------------------------------------------------------------- row pass --
+// TPR = R/8 threads per row, 8 elements each; a warp holds 32/TPR rows.
+// Per row: twist A and B, forward cyclic NTTs, Montgomery pointwise product,
+// inverse cyclic NTT, untwist (with the CRT weight), store into A's plane.
+constexpr int kRowWarps = 8;
+
+template <int RB, int PH>
+__device__ __forceinline__ void row_fwd_phase(uint32_t (&x)[8], uint32_t t, uint32_t p, const uint2* rf) {
+    constexpr PhaseMap<RB, 3> map(PH);
+    phase_ct<RB, 3>(x, map, t, p, [&](int level, uint32_t s) { return rf[(1u << level) + (s >> (RB - level))]; });
+}
+template <int RB, int PH>
+__device__ __forceinline__ void row_inv_phase(uint32_t (&x)[8], uint32_t t, uint32_t p, const uint2* ri) {
+    constexpr PhaseMap<RB, 3> map(PH);
+    phase_gs<RB, 3>(x, map, t, p, [&](int level, uint32_t s) { return ri[(1u << level) + (s >> (RB - level))]; });
+}
+template <int RB, int FROM, int TO>
+__device__ __forceinline__ void row_exchange(uint32_t (&x)[8], uint32_t* rowbuf, uint32_t t) {
+    constexpr PhaseMap<RB, 3> from(FROM), to(TO);
+#pragma unroll
+    for (uint32_t k = 0; k < 8; ++k) rowbuf[swz(from.index(t, k))] = x[k];
+    __syncwarp();
+#pragma unroll
+    for (uint32_t k = 0; k < 8; ++k) x[k] = rowbuf[swz(to.index(t, k))];
+    __syncwarp();
+}
+
+template <int RB>
+__device__ __forceinline__ void row_forward(uint32_t (&x)[8], uint32_t* rowbuf, uint32_t t, uint32_t p, const uint2* rf) {
+    constexpr int NPH = phase_count(RB);
+    row_fwd_phase<RB, 0>(x, t, p, rf);
+    if constexpr (NPH > 1) { row_exchange<RB, 0, 1>(x, rowbuf, t); row_fwd_phase<RB, 1>(x, t, p, rf); }
+    if constexpr (NPH > 2) { row_exchange<RB, 1, 2>(x, rowbuf, t); row_fwd_phase<RB, 2>(x, t, p, rf); }
+}
+template <int RB>
+__device__ __forceinline__ void row_inverse(uint32_t (&x)[8], uint32_t* rowbuf, uint32_t t, uint32_t p, const uint2* ri) {
+    constexpr int NPH = phase_count(RB);
+    if constexpr (NPH > 2) { row_inv_phase<RB, 2>(x, t, p, ri); row_exchange<RB, 2, 1>(x, rowbuf, t); }
+    if constexpr (NPH > 1) { row_inv_phase<RB, 1>(x, t, p, ri); row_exchange<RB, 1, 0>(x, rowbuf, t); }
+    row_inv_phase<RB, 0>(x, t, p, ri);
+}
+
+template <int RB>
+__global__ void __launch_bounds__(32 * kRowWarps)
+row_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t* planes_b, size_t b_stride,
+           uint32_t* planes_out, size_t out_stride, uint32_t rows_per_cta, uint32_t a_spectral) {
+    constexpr uint32_t R = 1u << RB;
+    constexpr uint32_t TPR = R / 8;
+    constexpr uint32_t RPW = 32 / TPR;
+    extern __shared__ uint4 smem_raw[];
+    uint2* tabs = reinterpret_cast<uint2*>(smem_raw);
+    const uint32_t Z = a.Z, H = a.H;
+    uint2* s_row_f = tabs;
+    uint2* s_row_i = s_row_f + R;
+    uint2* s_tw_lo = s_row_i + R;
+    uint2* s_tw_hi = s_tw_lo + Z;
+    uint2* s_itw_lo = s_tw_hi + H;
+    uint2* s_itw_hi = s_itw_lo + Z;
+    uint32_t* xbuf = reinterpret_cast<uint32_t*>(s_itw_hi + H);   // kRowWarps x 2 x 256 words
+
+    const uint32_t j = blockIdx.y;
+    const uint4 pc = a.consts[j];
+    const uint32_t p = pc.x, np = pc.z;
+    {
+        const uint2* g = a.tables + size_t(j) * a.table_stride;
+        for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) {
+            s_row_f[i] = g[a.off_row_f + i];
+            s_row_i[i] = g[a.off_row_i + i];
+        }
+        for (uint32_t i = threadIdx.x; i < Z; i += blockDim.x) {
+            s_tw_lo[i] = g[a.off_tw_lo + i];
+            s_itw_lo[i] = g[a.off_itw_lo + i];
+        }
+        for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
+            s_tw_hi[i] = g[a.off_tw_hi + i];
+            s_itw_hi[i] = g[a.off_itw_hi + i];
+        }
+    }
+    __syncthreads();
+
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t t = lane % TPR, rw = lane / TPR;
+    uint32_t* bufa = xbuf + warp * 512 + rw * R;
+    uint32_t* bufb = bufa + 256;
+    const uint32_t C = a.N / R;
+    const uint32_t zmask = Z - 1;
+    const size_t z = blockIdx.z, jn = size_t(j) * a.N;
+    constexpr PhaseMap<RB, 3> m0(0);
+    constexpr PhaseMap<RB, 3> ml(phase_count(RB) - 1);
+
+    for (uint32_t it = 0; it * (kRowWarps * RPW) < rows_per_cta; ++it) {
+        const uint32_t i2 = blockIdx.x * rows_per_cta + it * (kRowWarps * RPW) + warp * RPW + rw;
+        const bool valid = i2 < C && it * (kRowWarps * RPW) + warp * RPW + rw < rows_per_cta;
+        const uint32_t e0 = 2 * bit_reverse_dev(i2, a.c_bits) + 1;
+        const uint32_t* rowa = planes_a + z * a_stride + jn + size_t(i2) * R;
+        const uint32_t* rowb = planes_b + z * b_stride + jn + size_t(i2) * R;
+        uint32_t* rowo = planes_out + z * out_stride + jn + size_t(i2) * R;
+        uint32_t xa[8], xb[8];
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            // A cached in spectral form is stored in the forward transform's output order.
+            xa[k] = valid ? rowa[a_spectral ? ml.index(t, k) : m0.index(t, k)] : 0u;
+            xb[k] = valid ? rowb[m0.index(t, k)] : 0u;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            const uint32_t e = e0 * m0.index(t, k);
+            const uint2 lo = s_tw_lo[e & zmask], hi = s_tw_hi[e >> a.z_bits];
+            if (!a_spectral) xa[k] = mul_shoup(mul_shoup(xa[k], lo.x, lo.y, p), hi.x, hi.y, p);
+            xb[k] = mul_shoup(mul_shoup(xb[k], lo.x, lo.y, p), hi.x, hi.y, p);
+        }
+        if (!a_spectral) row_forward<RB>(xa, bufa, t, p, s_row_f);
+        row_forward<RB>(xb, bufb, t, p, s_row_f);
+        // Both operands now sit in the last phase's layout: pointwise product.
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) xa[k] = mul_mont(reduce_once(xa[k], p), xb[k], p, np);
+        row_inverse<RB>(xa, bufa, t, p, s_row_i);
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            const uint32_t s = m0.index(t, k);
+            const uint32_t e = e0 * s;
+            const uint2 lo = s_itw_lo[e & zmask], hi = s_itw_hi[e >> a.z_bits];
+            uint32_t v = mul_shoup(mul_shoup(xa[k], lo.x, lo.y, p), hi.x, hi.y, p);
+            // With a single row there is no inverse column pass: emit canonical terms here.
+            if (C == 1) v = reduce_once(v, p);
+            if (valid) rowo[s] = v;
+        }
+    }
+}
+
+// Forward row transform only (twist + cyclic NTT), in place: leaves an operand
+// in the spectral form that row_kernel accepts with a_spectral = 1.
+template <int RB>
+__global__ void __launch_bounds__(32 * kRowWarps)
+row_forward_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride, uint32_t rows_per_cta) {
+    constexpr uint32_t R = 1u << RB;
+    constexpr uint32_t TPR = R / 8;
+    constexpr uint32_t RPW = 32 / TPR;
+    extern __shared__ uint4 smem_raw[];
+    uint2* tabs = reinterpret_cast<uint2*>(smem_raw);
+    const uint32_t Z = a.Z, H = a.H;
+    uint2* s_row_f = tabs;
+    uint2* s_tw_lo = s_row_f + R;
+    uint2* s_tw_hi = s_tw_lo + Z;
+    uint32_t* xbuf = reinterpret_cast<uint32_t*>(s_tw_hi + H);
+    const uint32_t j = blockIdx.y;
+    const uint32_t p = a.consts[j].x;
+    {
+        const uint2* g = a.tables + size_t(j) * a.table_stride;
+        for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_row_f[i] = g[a.off_row_f + i];
+        for (uint32_t i = threadIdx.x; i < Z; i += blockDim.x) s_tw_lo[i] = g[a.off_tw_lo + i];
+        for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) s_tw_hi[i] = g[a.off_tw_hi + i];
+    }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t t = lane % TPR, rw = lane / TPR;
+    uint32_t* buf = xbuf + warp * 256 + rw * R;
+    const uint32_t C = a.N / R;
+    const uint32_t zmask = Z - 1;
+    const size_t plane_off = size_t(blockIdx.z) * plane_stride + size_t(j) * a.N;
+    constexpr PhaseMap<RB, 3> m0(0);
+    constexpr PhaseMap<RB, 3> ml(phase_count(RB) - 1);
+    for (uint32_t it = 0; it * (kRowWarps * RPW) < rows_per_cta; ++it) {
+        const uint32_t i2 = blockIdx.x * rows_per_cta + it * (kRowWarps * RPW) + warp * RPW + rw;
+        const bool valid = i2 < C && it * (kRowWarps * RPW) + warp * RPW + rw < rows_per_cta;
+        const uint32_t e0 = 2 * bit_reverse_dev(i2, a.c_bits) + 1;
+        uint32_t* row = planes + plane_off + size_t(i2) * R;
+        uint32_t x[8];
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) {
+            const uint32_t s = m0.index(t, k);
+            const uint32_t v = valid ? row[s] : 0u;
+            const uint32_t e = e0 * s;
+            const uint2 lo = s_tw_lo[e & zmask], hi = s_tw_hi[e >> a.z_bits];
+            x[k] = mul_shoup(mul_shoup(v, lo.x, lo.y, p), hi.x, hi.y, p);
+        }
+        row_forward<RB>(x, buf, t, p, s_row_f);
+        // Spectral values are stored in natural (bit-reversed evaluation) order.
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k)
+            if (valid) row[ml.index(t, k)] = x[k];
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers --
+template <bool INVERSE>
+static cudaError_t launch_col(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
+    const uint32_t C = a.N / 256;
+    if (C <= 1) return cudaSuccess;
+    const dim3 grid(256 / 32, a.P, nplanes);
+    switch (a.c_bits) {
+#define BCG_COL(CBV) case CBV: col_kernel<CBV, INVERSE><<<grid, 32 * ((1 << CBV) >> local_bits(CBV)), 0, st>>>(a, planes, stride); break;
+        BCG_COL(1) BCG_COL(2) BCG_COL(3) BCG_COL(4) BCG_COL(5) BCG_COL(6) BCG_COL(7) BCG_COL(8)
+#undef BCG_COL
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_col_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
+    return launch_col<false>(a, planes, stride, nplanes, st);
+}
+cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
+    return launch_col<true>(a, planes, stride, nplanes, st);
+}
+
+static uint32_t row_rows_per_cta(uint32_t C, uint32_t rows_per_iter) {
+    uint32_t rows = C < 32 ? C : 32;
+    if (rows < rows_per_iter) rows = rows_per_iter;
+    return rows;
+}
+
+size_t row_smem_bytes(const NttArgs& a, bool forward_only) {
+    const uint32_t R = a.N < 256 ? a.N : 256;
+    const size_t tabs = forward_only ? (R + a.Z + a.H) : (2 * R + 2 * a.Z + 2 * a.H);
+    return tabs * sizeof(uint2) + (forward_only ? 1 : 2) * kRowWarps * 256 * sizeof(uint32_t);
+}
+
+cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_t a_stride,
+                               const uint32_t* planes_b, size_t b_stride, uint32_t* planes_out,
+                               size_t out_stride, uint32_t nprod, bool a_spectral, cudaStream_t st) {
+    const uint32_t R = a.N < 256 ? a.N : 256;
+    const uint32_t C = a.N / R;
+    const uint32_t rpi = kRowWarps * (32 / (R / 8));
+    const uint32_t rows = row_rows_per_cta(C, rpi);
+    const dim3 grid((C + rows - 1) / rows, a.P, nprod);
+    const size_t smem = row_smem_bytes(a, false);
+    const uint32_t rb = 31 - __builtin_clz(R);
+    switch (rb) {
+#define BCG_ROW(RBV) case RBV: \
+        cudaFuncSetAttribute(row_kernel<RBV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
+        row_kernel<RBV><<<grid, 32 * kRowWarps, smem, st>>>(a, planes_a, a_stride, planes_b, b_stride, planes_out, out_stride, rows, a_spectral ? 1u : 0u); break;
+        BCG_ROW(4) BCG_ROW(5) BCG_ROW(6) BCG_ROW(7) BCG_ROW(8)
+#undef BCG_ROW
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
+    const uint32_t R = a.N < 256 ? a.N : 256;
+    const uint32_t C = a.N / R;
+    const uint32_t rpi = kRowWarps * (32 / (R / 8));
+    const uint32_t rows = row_rows_per_cta(C, rpi);
+    const dim3 grid((C + rows - 1) / rows, a.P, nplanes);
+    const size_t smem = row_smem_bytes(a, true);
+    const uint32_t rb = 31 - __builtin_clz(R);
+    switch (rb) {
+#define BCG_ROWF(RBV) case RBV: \
+        cudaFuncSetAttribute(row_forward_kernel<RBV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
+        row_forward_kernel<RBV><<<grid, 32 * kRowWarps, smem, st>>>(a, planes, stride, rows); break;
+        BCG_ROWF(4) BCG_ROWF(5) BCG_ROWF(6) BCG_ROWF(7) BCG_ROWF(8)
+#undef BCG_ROWF
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace bcg

@@ -1,0 +1,208 @@
+"""ctypes binding of libbytecrt_gb300.so (include/bytecrt_gb300.h).
+
+The product path is native only: if the shared library is missing this module
+raises, it never falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbytecrt_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "bytecrt_gb300.h")
+
+BCG_OK = 0
+BCG_ERR_INVALID = 1
+BCG_ERR_CUDA = 2
+BCG_ERR_NOMEM = 3
+BCG_ERR_DEVICE_TIMEOUT = 4
+BCG_ERR_BUSY = 5
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+
+
+class BcgError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"bcg error {code}: {message}")
+        self.code = code
+
+
+class bcg_info(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in
+                ("N", "W", "L", "P", "kpad", "enc_k", "enc_cols", "crt_k", "crt_n",
+                 "product_bits", "group", "reserved")] + [("workspace_bytes_per_product", ctypes.c_uint64)]
+
+
+class bcg_profile(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_double * 8), ("launches", ctypes.c_uint64 * 8), ("chains", ctypes.c_uint64)]
+
+
+STAGES = ("encode", "column", "row", "column_inverse", "crt")
+
+_lib = None
+
+
+def header_functions() -> list[str]:
+    """Names of every function declared in include/bytecrt_gb300.h."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(bcg_[a-z_0-9]+)\s*\(", text, re.M)))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"native library missing: {LIB_PATH} (run __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        L.bcg_last_error.restype = ctypes.c_char_p
+        vp = ctypes.c_void_p
+        L.bcg_plan_create.argtypes = [ctypes.c_uint32] * 3 + [_u32p, ctypes.POINTER(vp)]
+        L.bcg_plan_destroy.argtypes = [vp]
+        L.bcg_plan_destroy.restype = None
+        L.bcg_plan_info.argtypes = [vp, ctypes.POINTER(bcg_info)]
+        L.bcg_plan_primes.argtypes = [vp, _u32p, _u32p, _u32p]
+        L.bcg_plan_weights.argtypes = [vp, _u32p]
+        L.bcg_context_create.argtypes = [ctypes.c_uint32] * 3 + [_u32p, ctypes.c_int, ctypes.POINTER(vp)]
+        L.bcg_context_destroy.argtypes = [vp]
+        L.bcg_context_destroy.restype = None
+        L.bcg_context_info.argtypes = [vp, ctypes.POINTER(bcg_info)]
+        L.bcg_multiply.argtypes = [vp, _u32p, _u32p, _u32p, ctypes.c_uint32]
+        L.bcg_multiply_device.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
+        L.bcg_encode_device.argtypes = [vp, vp, vp, vp, vp, ctypes.c_size_t, ctypes.c_uint32, vp]
+        L.bcg_negacyclic_device.argtypes = [vp, vp, vp, ctypes.c_size_t, ctypes.c_uint32, vp]
+        L.bcg_crt_device.argtypes = [vp, vp, ctypes.c_size_t, vp, ctypes.c_uint32, vp]
+        L.bcg_synchronize.argtypes = [vp]
+        L.bcg_profile_enable.argtypes = [vp, ctypes.c_int]
+        L.bcg_profile_read.argtypes = [vp, ctypes.POINTER(bcg_profile), ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != BCG_OK:
+        raise BcgError(rc, lib().bcg_last_error().decode())
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.uint32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_u32p)
+
+
+def _ptr(x) -> int | None:
+    """Device pointer of a torch tensor (or an int address)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def limbs(W: int) -> int:
+    return (W + 31) // 32
+
+
+class Plan:
+    """Host-only plan (no GPU needed)."""
+
+    def __init__(self, N: int, W: int, q):
+        self.N, self.W, self.L = int(N), int(W), limbs(W)
+        q = np.ascontiguousarray(q, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        _check(lib().bcg_plan_create(self.N, self.W, self.L, _p(q), ctypes.byref(h)))
+        self._h = h
+        info = bcg_info()
+        _check(lib().bcg_plan_info(self._h, ctypes.byref(info)))
+        self.info = info
+        self.P = info.P
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().bcg_plan_destroy(self._h)
+            self._h = None
+
+    def primes(self):
+        p, s, c = (np.zeros(self.P, np.uint32) for _ in range(3))
+        _check(lib().bcg_plan_primes(self._h, _p(p), _p(s), _p(c)))
+        return p, s, c
+
+    def weights(self):
+        w = np.zeros((self.P + 1) * self.L, np.uint32)
+        _check(lib().bcg_plan_weights(self._h, _p(w)))
+        return w.reshape(self.P + 1, self.L)
+
+
+class Multiplier:
+    """One point (N, W, q) on one GPU: the native context behind fherma_init."""
+
+    def __init__(self, N: int, W: int, q, device: int = 0):
+        self.N, self.W, self.L = int(N), int(W), limbs(W)
+        self.q = np.ascontiguousarray(q, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        _check(lib().bcg_context_create(self.N, self.W, self.L, _p(self.q), int(device), ctypes.byref(h)))
+        self._h = h
+        info = bcg_info()
+        _check(lib().bcg_context_info(self._h, ctypes.byref(info)))
+        self.info = info
+        self.P = info.P
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bcg_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def plane_words(self) -> int:
+        return self.P * self.N
+
+    # ---- host buffers
+    def multiply(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        a = np.ascontiguousarray(a, dtype=np.uint32)
+        b = np.ascontiguousarray(b, dtype=np.uint32)
+        if a.shape != b.shape or a.size % (self.N * self.L):
+            raise ValueError("operands must be [count][N][L] uint32 of equal shape")
+        count = a.size // (self.N * self.L)
+        c = np.zeros_like(a)
+        _check(lib().bcg_multiply(self._h, _p(a), _p(b), _p(c), count))
+        return c
+
+    def multiply_into(self, a, b, c, count: int):
+        """Host buffers given as addresses (e.g. pinned torch tensors): c = a*b, synchronous."""
+        vp = ctypes.c_void_p
+        _check(lib().bcg_multiply(self._h, ctypes.cast(vp(_ptr(a)), _u32p), ctypes.cast(vp(_ptr(b)), _u32p),
+                                  ctypes.cast(vp(_ptr(c)), _u32p), count))
+
+    # ---- device buffers (torch tensors or raw addresses)
+    def multiply_device(self, a, b, c, count: int, stream=None):
+        _check(lib().bcg_multiply_device(self._h, _ptr(a), _ptr(b), _ptr(c), count, _ptr(stream)))
+
+    def encode_device(self, a, b, planes_a, planes_b, plane_stride: int, count: int, stream=None):
+        _check(lib().bcg_encode_device(self._h, _ptr(a), _ptr(b), _ptr(planes_a), _ptr(planes_b),
+                                       plane_stride, count, _ptr(stream)))
+
+    def negacyclic_device(self, planes_a, planes_b, plane_stride: int, count: int, stream=None):
+        _check(lib().bcg_negacyclic_device(self._h, _ptr(planes_a), _ptr(planes_b), plane_stride, count,
+                                           _ptr(stream)))
+
+    def crt_device(self, terms, plane_stride: int, c, count: int, stream=None):
+        _check(lib().bcg_crt_device(self._h, _ptr(terms), plane_stride, _ptr(c), count, _ptr(stream)))
+
+    def synchronize(self):
+        _check(lib().bcg_synchronize(self._h))
+
+    # ---- measurement
+    def profile(self, enable: bool = True):
+        _check(lib().bcg_profile_enable(self._h, 1 if enable else 0))
+
+    def read_profile(self, reset: bool = True) -> dict:
+        p = bcg_profile()
+        _check(lib().bcg_profile_read(self._h, ctypes.byref(p), 1 if reset else 0))
+        return {"ms": {s: p.ms[i] for i, s in enumerate(STAGES)},
+                "launches": {s: int(p.launches[i]) for i, s in enumerate(STAGES)},
+                "chains": int(p.chains)}

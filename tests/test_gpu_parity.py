@@ -1,0 +1,177 @@
+"""GPU parity: every stage and the whole product, through the C ABI, bit-exact
+against the CPU oracle (oracle/oracle.c, pinned to the reference)."""
+import numpy as np
+import pytest
+
+from conftest import package
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def dev(x: np.ndarray):
+    return torch.from_numpy(np.ascontiguousarray(x).view(np.int32)).cuda()
+
+
+def host(t) -> np.ndarray:
+    return t.cpu().numpy().view(np.uint32)
+
+
+def empty(words: int):
+    return torch.zeros(words, dtype=torch.int32, device="cuda")
+
+
+_cache = {}
+
+
+def setup(N, W, seed):
+    key = (N, W, seed)
+    if key not in _cache:
+        pkg = package()
+        q = pkg.inputs.modulus(W, seed)
+        _cache[key] = (pkg.Multiplier(N, W, q), O.Oracle(N, W, q), q)
+    return _cache[key]
+
+
+SMALL = [(16, 40), (64, 100), (256, 434), (512, 868), (2048, 300), (4096, 1747)]
+FULL = [(16384, 434), (32768, 868), (65536, 1747)]
+
+
+@pytest.mark.parametrize("N,W", SMALL + FULL)
+def test_encode_matches_oracle(N, W):
+    pkg = package()
+    m, o, q = setup(N, W, 1)
+    a = pkg.inputs.uniform(q, N, 11)
+    b = pkg.inputs.fixture(q, N, "minus_one")
+    pw = m.plane_words
+    pa, pb = empty(pw), empty(pw)
+    m.encode_device(dev(a), dev(b), pa, pb, pw, 1)
+    m.synchronize()
+    p = o.primes.astype(np.uint64)[:, None]
+    for x, planes in ((a, pa), (b, pb)):
+        got = host(planes).reshape(o.P, N).astype(np.uint64)
+        assert (got < 2 * p).all()
+        assert np.array_equal(got % p, o.encode(x).astype(np.uint64))
+
+
+@pytest.mark.parametrize("N,W", SMALL + FULL)
+def test_negacyclic_terms_match_oracle(N, W):
+    pkg = package()
+    m, o, q = setup(N, W, 2)
+    a = pkg.inputs.uniform(q, N, 21)
+    b = pkg.inputs.uniform(q, N, 22)
+    ra, rb = o.encode(a), o.encode(b)
+    pw = m.plane_words
+    pa, pb = dev(ra.reshape(-1)), dev(rb.reshape(-1))
+    m.negacyclic_device(pa, pb, pw, 1)
+    m.synchronize()
+    got = host(pa).reshape(o.P, N)
+    primes, cinv = o.primes, o.crt_inverse
+    for j in ([0, 1, o.P // 2, o.P - 1] if N >= 16384 else range(o.P)):
+        want = o.prime_product(j, ra[j], rb[j]).astype(np.uint64) * int(cinv[j]) % int(primes[j])
+        assert np.array_equal(got[j].astype(np.uint64), want), f"prime {j}"
+
+
+@pytest.mark.parametrize("N,W", SMALL + FULL)
+def test_crt_matches_oracle(N, W):
+    pkg = package()
+    m, o, q = setup(N, W, 3)
+    a = pkg.inputs.uniform(q, N, 31)
+    b = pkg.inputs.uniform(q, N, 32)
+    ra, rb = o.encode(a), o.encode(b)
+    prods = np.stack([o.prime_product(j, ra[j], rb[j]) for j in range(o.P)])
+    terms = (prods.astype(np.uint64) * o.crt_inverse.astype(np.uint64)[:, None]
+             % o.primes.astype(np.uint64)[:, None]).astype(np.uint32)
+    c = empty(N * m.L)
+    m.crt_device(dev(terms.reshape(-1)), m.plane_words, c, 1)
+    m.synchronize()
+    assert np.array_equal(host(c).reshape(N, m.L), o.crt(prods))
+
+
+@pytest.mark.parametrize("N,W", SMALL + FULL)
+def test_multiply_device_matches_oracle(N, W):
+    pkg = package()
+    m, o, q = setup(N, W, 4)
+    a = pkg.inputs.uniform(q, N, 41)
+    b = pkg.inputs.uniform(q, N, 42)
+    c = empty(N * m.L)
+    m.multiply_device(dev(a), dev(b), c, 1)
+    m.synchronize()
+    assert np.array_equal(host(c).reshape(N, m.L), o.multiply(a, b))
+
+
+@pytest.mark.parametrize("kind_a,kind_b", [("zero", "random"), ("one", "random"), ("minus_one", "minus_one"),
+                                           ("half_low", "half_high"), ("half_high", "half_high"),
+                                           ("minus_one", "one")])
+@pytest.mark.parametrize("N,W", [(1024, 868), (32768, 868)])
+def test_edge_fixtures(N, W, kind_a, kind_b):
+    pkg = package()
+    m, o, q = setup(N, W, 5)
+    pick = lambda kind, s: pkg.inputs.uniform(q, N, s) if kind == "random" else pkg.inputs.fixture(q, N, kind)
+    a, b = pick(kind_a, 51), pick(kind_b, 52)
+    got = m.multiply(a, b)
+    assert np.array_equal(got, o.multiply(a, b))
+
+
+@pytest.mark.parametrize("seed", [101, 102, 103])
+def test_full_size_three_moduli(seed):
+    """N=65536, W=1747 (L=55, P=114) with three seeded 1747-bit moduli."""
+    pkg = package()
+    N, W = 65536, 1747
+    q = pkg.inputs.modulus(W, seed)
+    m = pkg.Multiplier(N, W, q)
+    o = O.Oracle(N, W, q)
+    a, b = pkg.inputs.uniform(q, N, seed * 3), pkg.inputs.uniform(q, N, seed * 3 + 1)
+    assert np.array_equal(m.multiply(a, b), o.multiply(a, b))
+    m.close()
+
+
+@pytest.mark.parametrize("gap", [1, 2 * 65536 - 1, (1 << 32) - 1])
+def test_gap_form_moduli(gap):
+    """The reference's own modulus form q = 2^W - gap at its main geometry."""
+    pkg = package()
+    N, W = 65536, 1747
+    q = pkg.inputs.gap_modulus(W, gap)
+    m = pkg.Multiplier(N, W, q)
+    o = O.Oracle(N, W, q)
+    a, b = pkg.inputs.uniform(q, N, gap % 1000), pkg.inputs.fixture(q, N, "minus_one")
+    assert np.array_equal(m.multiply(a, b), o.multiply(a, b))
+    m.close()
+
+
+def test_batch_equals_single_products():
+    pkg = package()
+    N, W, B = 16384, 434, 7
+    m, o, q = setup(N, W, 6)
+    a = np.stack([pkg.inputs.uniform(q, N, 600 + i) for i in range(B)])
+    b = np.stack([pkg.inputs.uniform(q, N, 700 + i) for i in range(B)])
+    batched = m.multiply(a, b)
+    for i in (0, 3, B - 1):
+        assert np.array_equal(batched[i], m.multiply(a[i], b[i]))
+        assert np.array_equal(batched[i], o.multiply(a[i], b[i]))
+
+
+def test_repeated_calls_are_deterministic():
+    pkg = package()
+    N, W = 32768, 868
+    m, o, q = setup(N, W, 7)
+    a, b = pkg.inputs.uniform(q, N, 1), pkg.inputs.uniform(q, N, 2)
+    first = m.multiply(a, b)
+    for _ in range(3):
+        assert np.array_equal(m.multiply(a, b), first)
+
+
+def test_plugin_abi_roundtrip():
+    pkg = package()
+    N, W = 16384, 434
+    q = pkg.inputs.modulus(W, 8)
+    st = pkg.fherma_init(pkg.Point(N=N, W=W, L=14, q=q))
+    a, b = pkg.inputs.uniform(q, N, 1), pkg.inputs.uniform(q, N, 2)
+    out = pkg.fherma_run(st, pkg.Inputs(a=a, b=b))
+    assert out.c.shape == (N, 14)
+    assert np.array_equal(out.c, O.Oracle(N, W, q).multiply(a, b))
+    with pytest.raises(RuntimeError):
+        pkg.fherma_run(st, pkg.Inputs(a=a[:-1], b=b))
+    pkg.fherma_free(st)
