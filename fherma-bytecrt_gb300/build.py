@@ -67,19 +67,23 @@ def build(verbose: bool = False) -> str:
         subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fopenmp", "-lgomp"],
                        check=True)
         os.replace(tmp, LIB)
+    # The plugin ABI twice: single product and batched (Point carries B).
+    inc = ["-I", os.path.join(REPO, "include")]
     shim_src = os.path.join(CSRC, "fherma_shim.cpp")
-    if os.path.exists(shim_src) and _stale(SHIM, [shim_src, LIB, *_headers()]):
-        tmp = SHIM + f".tmp{os.getpid()}"
-        subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", os.path.join(REPO, "include"),
-                        "-o", tmp, shim_src, "-L", HERE, "-lbytecrt_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
-        os.replace(tmp, SHIM)
     harness_src = os.path.join(CSRC, "harness.cpp")
-    if os.path.exists(harness_src) and os.path.exists(SHIM) and _stale(HARNESS, [harness_src, SHIM]):
-        tmp = HARNESS + f".tmp{os.getpid()}"
-        subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(REPO, "include"), "-o", tmp,
-                        harness_src, "-L", HERE, "-lfherma_gb300", "-lbytecrt_gb300",
-                        "-Wl,-rpath,$ORIGIN"], check=True)
-        os.replace(tmp, HARNESS)
+    for suffix, defs in (("", []), ("_batched", ["-DFHERMA_BATCHED"])):
+        shim = os.path.join(HERE, f"libfherma_gb300{suffix}.so")
+        if _stale(shim, [shim_src, LIB, *_headers()]):
+            tmp = shim + f".tmp{os.getpid()}"
+            subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", *defs, *inc, "-o", tmp, shim_src,
+                            "-L", HERE, "-lbytecrt_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
+            os.replace(tmp, shim)
+        harness = os.path.join(HERE, f"solution{suffix}")
+        if _stale(harness, [harness_src, shim, *_headers()]):
+            tmp = harness + f".tmp{os.getpid()}"
+            subprocess.run(["g++", "-std=c++17", "-O2", *defs, *inc, "-o", tmp, harness_src, "-L", HERE,
+                            f"-lfherma_gb300{suffix}", "-lbytecrt_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
+            os.replace(tmp, harness)
     return LIB
 
 

@@ -114,6 +114,45 @@ int bcg_context_info(const bcg_context* ctx, bcg_info* out) {
     });
 }
 
+int bcg_context_set_group(bcg_context* ctx, uint32_t group) {
+    return guarded([&] {
+        require(ctx && group >= 1 && group <= 4096, "group must be in [1, 4096]");
+        ctx->ctx->set_group(group);
+    });
+}
+
+int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
+    return guarded([&] {
+        require(ctx && knob, "null argument");
+        const std::string k(knob);
+        auto& c = *ctx->ctx;
+        if (k == "group") {
+            require(value >= 1 && value <= 4096, "group must be in [1, 4096]");
+            c.set_group(uint32_t(value));
+        } else if (k == "encode_bstages") {
+            require(value == 2 || value == 3, "encode_bstages must be 2 or 3");
+            c.encode_tuning().bstages = uint32_t(value);
+        } else if (k == "encode_accbuf") {
+            require(value == 2 || value == 4, "encode_accbuf must be 2 or 4");
+            c.encode_tuning().accbuf = uint32_t(value);
+        } else {
+            throw std::invalid_argument("unknown tuning knob: " + k);
+        }
+    });
+}
+
+int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* value) {
+    return guarded([&] {
+        require(ctx && knob && value, "null argument");
+        const std::string k(knob);
+        auto& c = *ctx->ctx;
+        if (k == "group") *value = c.group();
+        else if (k == "encode_bstages") *value = c.encode_tuning().bstages;
+        else if (k == "encode_accbuf") *value = c.encode_tuning().accbuf;
+        else throw std::invalid_argument("unknown tuning knob: " + k);
+    });
+}
+
 int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count) {
     return guarded([&] {
         require(ctx, "null context");

@@ -163,6 +163,11 @@ __device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, 
         :: "r"(smem_u32(smem_dst)), "l"(gmem_src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
+// Hint: bring [src, src + bytes) into L2 ahead of a later bulk copy.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* gmem_src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(gmem_src), "r"(bytes) : "memory");
+}
+
 // Generic-proxy writes to shared memory become visible to the async proxy
 // (tensor core operand reads) after this fence.
 __device__ __forceinline__ void fence_proxy_async() {

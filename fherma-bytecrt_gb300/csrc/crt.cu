@@ -10,8 +10,13 @@
 // Each term is split into 4 balanced byte digits and each (256^a * W_u) mod q
 // into crt_e balanced byte digits, so z = sum_e S_e 256^e where the digit sums
 // S_e (|S_e| <= 4(P+1)*128*128 < 2^24) come exact from one fp32-accumulating
-// MMA [128 x 4(P+1)] x [4(P+1) x crt_e].  This is the reference's four-column
+// MMA [256 x 4(P+1)] x [4(P+1) x crt_e].  This is the reference's four-column
 // B4 algebra (native-smoke/README.md, g1-crt.cuh:201-335) with signed digits.
+//
+// Per K chunk (16 terms) one thread issues two bulk copies into a stage: the
+// chunk of the weight-digit matrix, and the 16 t_j plane rows of the CTA's 256
+// coefficients (1 KB each).  Eight producer warps (thread = coefficient row)
+// turn the staged t_j into fp16 digits of the A tile and accumulate alpha.
 //
 // Epilogue per row (TMEM lane): signed 64-bit carry chain over the limbs, then
 // a generic reduction mod q (the reference's reducer only handles
@@ -25,14 +30,17 @@ namespace bcg {
 namespace {
 
 constexpr uint32_t kTileRows = 128;
-constexpr uint32_t kCrtThreads = 160;
-constexpr uint32_t kCrtTmemCols = 256;
+constexpr uint32_t kTiles = 2;
+constexpr uint32_t kRows = kTileRows * kTiles;
+constexpr uint32_t kProdWarps = 8;
+constexpr uint32_t kCrtThreads = (kProdWarps + 1) * 32;
+constexpr uint32_t kTermsPerChunk = kCrtChunkK / 4;      // 8
+constexpr uint32_t kStages = 4;
 
 struct CrtSmem {
-    uint64_t afull[2], bfull[2], sempty[2], accfull;
+    uint64_t afull[kStages], bfull[kStages], sempty[kStages], accfull;
     uint32_t tmem_base;
     uint32_t abort_flag;
-    uint32_t q[64];
 };
 
 __device__ __forceinline__ uint32_t chunk_k(uint32_t k_total, uint32_t kc) {
@@ -40,29 +48,161 @@ __device__ __forceinline__ uint32_t chunk_k(uint32_t k_total, uint32_t kc) {
     return rem >= kCrtChunkK ? kCrtChunkK : (rem + 15) / 16 * 16;
 }
 
+
+// One limb of the carry chain: S_0 + 256 S_1 + 2^16 S_2 + 2^24 S_3 + carry.
+// With |S| < 2^23 and P < 127 the partial sums u, v fit int32; otherwise 64-bit.
+__device__ __forceinline__ int64_t limb_value(float f0, float f1, float f2, float f3, bool narrow) {
+    const int32_t s0 = __float2int_rn(f0), s1 = __float2int_rn(f1);
+    const int32_t s2 = __float2int_rn(f2), s3 = __float2int_rn(f3);
+    if (narrow) {
+        const int32_t u = s3 * 256 + s2, v = s1 * 256 + s0;
+        return int64_t(u) * 65536 + v;
+    }
+    return (int64_t(s3) << 24) + (int64_t(s2) << 16) + (int64_t(s1) << 8) + s0;
+}
+
+// Reduces the signed (L+1)-word value (z, top) mod q in place.  k is the
+// floor of the quotient estimated in double precision from the top words
+// (error far below 1), so after z - k q at most one correction remains.
+template <int LT>
+__device__ __forceinline__ void reduce_mod_q(uint32_t* z, int64_t top, const CrtArgs& a, uint32_t L) {
+    double zhi = double(top);
+    const uint32_t T = L < 3 ? L : 3;     // q_inv_scaled = 2^(32(L-T)) / q
+#pragma unroll
+    for (uint32_t tt = 0; tt < 3; ++tt)
+        if (tt < T) zhi = zhi * 4294967296.0 + double(z[L - 1 - tt]);
+    const int64_t k = int64_t(floor(zhi * a.q_inv_scaled));
+    const bool neg = k < 0;
+    const uint32_t ka = uint32_t(neg ? -k : k);
+    int64_t c = 0;
+#pragma unroll
+    for (uint32_t l = 0; l < (LT ? LT : L); ++l) {
+        const int64_t prod = int64_t(uint64_t(ka) * a.q[l]);
+        const int64_t sum = int64_t(z[l]) + (neg ? prod : -prod) + c;
+        z[l] = uint32_t(sum);
+        c = sum >> 32;
+    }
+    top += c;
+    if (top < 0) {
+        uint64_t cc = 0;
+#pragma unroll
+        for (uint32_t l = 0; l < (LT ? LT : L); ++l) {
+            const uint64_t sum = uint64_t(z[l]) + a.q[l] + cc;
+            z[l] = uint32_t(sum);
+            cc = sum >> 32;
+        }
+    } else {
+        // d = z - q; keep d unless it borrowed out of the top word.
+        int64_t b = 0;
+        uint32_t d[LT ? LT : 1];
+        if constexpr (LT > 0) {
+#pragma unroll
+            for (uint32_t l = 0; l < LT; ++l) {
+                const int64_t sum = int64_t(z[l]) - int64_t(a.q[l]) + b;
+                d[l] = uint32_t(sum);
+                b = sum >> 32;
+            }
+            if (top + b >= 0) {
+#pragma unroll
+                for (uint32_t l = 0; l < LT; ++l) z[l] = d[l];
+            }
+        } else {
+            bool ge = top > 0;
+            if (!ge) {
+                ge = true;
+                for (int l = int(L) - 1; l >= 0; --l)
+                    if (z[l] != a.q[l]) { ge = z[l] > a.q[l]; break; }
+            }
+            if (ge) {
+                for (uint32_t l = 0; l < L; ++l) {
+                    const int64_t sum = int64_t(z[l]) - int64_t(a.q[l]) + b;
+                    z[l] = uint32_t(sum);
+                    b = sum >> 32;
+                }
+            }
+        }
+    }
+}
+
+// Carry chain over the row's TMEM accumulators, reduction mod q, result to
+// the shared staging row.  LT > 0: the limbs stay in registers.
+template <int LT>
+__device__ __forceinline__ void crt_row_epilogue(const CrtArgs& a, uint32_t taddr, uint32_t* zrow, bool valid) {
+    const uint32_t L = LT ? uint32_t(LT) : a.L;
+    const bool narrow = uint64_t(4) * (a.P + 1) * 16384u * 257u < (uint64_t(1) << 31);
+    const bool extra = a.E == 4 * L + 1;
+    int64_t carry = 0;
+    if constexpr (LT > 0) {
+        uint32_t z[LT];
+        constexpr uint32_t NB = (4 * LT + 1 + 31) / 32;
+#pragma unroll
+        for (uint32_t cb = 0; cb < NB; ++cb) {
+            float v[32];
+            tmem_ld32(taddr + cb * 32, v);
+#pragma unroll
+            for (uint32_t q4 = 0; q4 < 8; ++q4) {
+                const uint32_t l = cb * 8 + q4;
+                if (l < LT) {
+                    const int64_t sum = limb_value(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3], narrow) + carry;
+                    z[l] = uint32_t(sum);
+                    carry = sum >> 32;
+                } else if (l == LT && extra) {
+                    carry += int64_t(__float2int_rn(v[4 * q4]));
+                }
+            }
+        }
+        if (valid) reduce_mod_q<LT>(z, carry, a, L);
+#pragma unroll
+        for (uint32_t l = 0; l < LT; ++l) zrow[l] = z[l];
+    } else {
+        uint32_t* z = zrow;
+        for (uint32_t cb = 0; cb < (a.E + 31) / 32; ++cb) {
+            float v[32];
+            tmem_ld32(taddr + cb * 32, v);
+#pragma unroll
+            for (uint32_t q4 = 0; q4 < 8; ++q4) {
+                const uint32_t l = cb * 8 + q4;
+                if (l < L) {
+                    const int64_t sum = limb_value(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3], narrow) + carry;
+                    z[l] = uint32_t(sum);
+                    carry = sum >> 32;
+                } else if (l == L && extra) {
+                    carry += int64_t(__float2int_rn(v[4 * q4]));
+                }
+            }
+        }
+        if (valid) reduce_mod_q<0>(z, carry, a, L);
+    }
+}
+
+template <int LT>
 __global__ void __launch_bounds__(kCrtThreads, 1)
-crt_kernel(CrtArgs a) {
+crt_kernel(const __grid_constant__ CrtArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const uint32_t NC = a.NC;
-    const uint32_t a_bytes = kTileRows * kCrtChunkK * 2;
+    const uint32_t a_bytes = kRows * kCrtChunkK * 2;              // both tiles
     const uint32_t b_bytes = NC * kCrtChunkK * 2;
-    uint8_t* stageA = smem;                          // 2 x a_bytes
-    uint8_t* stageB = smem + 2 * a_bytes;            // 2 x b_bytes
-    CrtSmem* ctl = reinterpret_cast<CrtSmem*>(stageB + 2 * b_bytes);
-    uint32_t* zbuf = reinterpret_cast<uint32_t*>(smem);   // epilogue staging (after all MMAs)
+    const uint32_t t_bytes = kTermsPerChunk * kRows * 4;
+    const uint32_t stage_bytes = a_bytes + b_bytes + t_bytes;
+    CrtSmem* ctl = reinterpret_cast<CrtSmem*>(smem + kStages * stage_bytes);
+    uint32_t* zbuf = reinterpret_cast<uint32_t*>(smem);          // epilogue staging (after all MMAs)
     volatile uint32_t* abort_flag = &ctl->abort_flag;
+    auto stageA = [&](uint32_t s) { return smem + s * stage_bytes; };
+    auto stageB = [&](uint32_t s) { return smem + s * stage_bytes + a_bytes; };
+    auto stageT = [&](uint32_t s) { return reinterpret_cast<uint32_t*>(smem + s * stage_bytes + a_bytes + b_bytes); };
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t prod = blockIdx.y;
-    const uint32_t row0 = blockIdx.x * kTileRows;
+    const uint32_t row0 = blockIdx.x * kRows;
     const uint32_t* terms = a.terms + size_t(prod) * a.terms_stride;
     uint32_t* out = a.out + size_t(prod) * a.out_stride;
     const uint32_t L = a.L, P = a.P, N = a.N;
     const uint32_t nkc = a.kchunks;
+    const uint32_t rows = N - row0 < kRows ? N - row0 : kRows;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 2; ++i) {
-            mbar_init(&ctl->afull[i], kTileRows);
+        for (int i = 0; i < int(kStages); ++i) {
+            mbar_init(&ctl->afull[i], kRows);
             mbar_init(&ctl->bfull[i], 1);
             mbar_init(&ctl->sempty[i], 1);
         }
@@ -70,9 +210,10 @@ crt_kernel(CrtArgs a) {
         ctl->abort_flag = 0;
         mbar_fence_init();
     }
-    for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) ctl->q[l] = a.q[l];
-    if (warp == 4) {
-        tmem_alloc(&ctl->tmem_base, kCrtTmemCols);
+    // Two tile accumulators of NC fp32 columns each.
+    const uint32_t tile_cols = NC <= 128 ? 128u : 256u;
+    if (warp == kProdWarps) {
+        tmem_alloc(&ctl->tmem_base, 2 * tile_cols);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -80,150 +221,107 @@ crt_kernel(CrtArgs a) {
     tc_fence_after();
     const uint32_t tmem = ctl->tmem_base;
 
-    if (warp == 4) {
+    if (warp == kProdWarps) {
         if (lane == 0) {
-            auto load_b = [&](uint32_t kc) {
-                const uint32_t bytes = NC * chunk_k(a.k_total, kc) * 2;
-                mbar_arrive_expect_tx(&ctl->bfull[kc & 1], bytes);
-                bulk_load(stageB + (kc & 1) * b_bytes, a.crt_b + size_t(kc) * kCrtChunkK * NC, bytes,
-                          &ctl->bfull[kc & 1]);
+            // Stage s for chunk kc: weight digits + the staged t_j rows, one barrier.
+            auto load = [&](uint32_t kc) {
+                const uint32_t s = kc % kStages;
+                const uint32_t bb = NC * chunk_k(a.k_total, kc) * 2;
+                const uint32_t j0 = kc * kTermsPerChunk;
+                const uint32_t nj = j0 < P ? min(kTermsPerChunk, P - j0) : 0u;
+                mbar_arrive_expect_tx(&ctl->bfull[s], bb + nj * rows * 4);
+                bulk_load(stageB(s), a.crt_b + size_t(kc) * kCrtChunkK * NC, bb, &ctl->bfull[s]);
+                for (uint32_t jj = 0; jj < nj; ++jj)
+                    bulk_load(stageT(s) + jj * kRows, terms + size_t(j0 + jj) * N + row0, rows * 4, &ctl->bfull[s]);
             };
-            load_b(0);
-            if (nkc > 1) load_b(1);
+            for (uint32_t kc = 0; kc < kStages && kc < nkc; ++kc) load(kc);
             const uint32_t idesc = idesc_f16_f32(kTileRows, NC);
             bool ok = true;
             for (uint32_t kc = 0; ok && kc < nkc; ++kc) {
-                ok = mbar_wait(&ctl->afull[kc & 1], (kc >> 1) & 1, abort_flag, a.status);
-                if (ok) ok = mbar_wait(&ctl->bfull[kc & 1], (kc >> 1) & 1, abort_flag, a.status);
+                const uint32_t s = kc % kStages, sp = (kc / kStages) & 1;
+                ok = mbar_wait(&ctl->afull[s], sp, abort_flag, a.status);
+                if (ok) ok = mbar_wait(&ctl->bfull[s], sp, abort_flag, a.status);
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t kl = chunk_k(a.k_total, kc);
                 const uint32_t sbo = (kl / 8) * 128;
-                const uint32_t a_addr = smem_u32(stageA + (kc & 1) * a_bytes);
-                const uint32_t b_addr = smem_u32(stageB + (kc & 1) * b_bytes);
-                for (uint32_t ks = 0; ks < kl / 16; ++ks)
-                    mma_f16(tmem, smem_desc(a_addr + ks * 256, 128, sbo), smem_desc(b_addr + ks * 256, 128, sbo),
-                            idesc, (kc | ks) != 0);
-                mma_commit(&ctl->sempty[kc & 1]);
-                if (kc >= 1 && kc + 1 < nkc) {
-                    ok = mbar_wait(&ctl->sempty[(kc - 1) & 1], ((kc - 1) >> 1) & 1, abort_flag, a.status);
-                    if (ok) load_b(kc + 1);
+                const uint32_t b_addr = smem_u32(stageB(s));
+                for (uint32_t t = 0; t < kTiles; ++t) {
+                    const uint32_t a_addr = smem_u32(stageA(s)) + t * kTileRows * kl * 2;
+                    for (uint32_t ks = 0; ks < kl / 16; ++ks)
+                        mma_f16(tmem + t * tile_cols, smem_desc(a_addr + ks * 256, 128, sbo),
+                                smem_desc(b_addr + ks * 256, 128, sbo), idesc, (kc | ks) != 0);
+                }
+                mma_commit(&ctl->sempty[s]);
+                if (kc >= 1 && kc - 1 + kStages < nkc) {
+                    // Chunk kc-1's MMAs retired: its stage (A, B and t_j) takes chunk kc-1+kStages.
+                    const uint32_t pc = kc - 1;
+                    ok = mbar_wait(&ctl->sempty[pc % kStages], (pc / kStages) & 1, abort_flag, a.status);
+                    if (ok) load(pc + kStages);
                 }
             }
             mma_commit(&ctl->accfull);
+            mbar_wait(&ctl->accfull, 0, abort_flag, a.status);
         }
         __syncwarp();
     } else {
-        const uint32_t r = threadIdx.x;
-        const uint32_t i = row0 + r;
-        const bool valid = i < N;
+        const uint32_t r = threadIdx.x;                    // 0..255
+        const uint32_t tile = r / kTileRows, trow = r % kTileRows;
+        const bool valid = r < rows;
         float acc = 0.0f;
         bool ok = true;
         // ---- producer: balanced digits of t_j and alpha, 16 terms per K chunk.
-        for (uint32_t kc = 0; kc < nkc; ++kc) {
-            if (kc >= 2) ok = mbar_wait(&ctl->sempty[kc & 1], ((kc >> 1) - 1) & 1, abort_flag, a.status);
+        for (uint32_t kc = 0; ok && kc < nkc; ++kc) {
+            const uint32_t s = kc % kStages;
+            // bfull(kc) also implies chunk kc-kStages retired, so the A stage is free.
+            ok = mbar_wait(&ctl->bfull[s], (kc / kStages) & 1, abort_flag, a.status);
             if (!ok) break;
-            uint8_t* tile = stageA + (kc & 1) * a_bytes;
             const uint32_t kl = chunk_k(a.k_total, kc);
-            for (uint32_t pp = 0; pp < kl / 8; ++pp) {
+            uint8_t* tileA = stageA(s) + tile * kTileRows * kl * 2;
+            const uint32_t* ts = stageT(s) + r;
+            uint32_t t[kTermsPerChunk];
+#pragma unroll
+            for (uint32_t jj = 0; jj < kTermsPerChunk; ++jj) {
+                const uint32_t u = kc * kTermsPerChunk + jj;
+                t[jj] = (u < P && valid) ? ts[jj * kRows] : 0u;
+            }
+#pragma unroll
+            for (uint32_t jj = 0; jj < kTermsPerChunk; ++jj) {
+                const uint32_t u = kc * kTermsPerChunk + jj;
+                if (u < P) acc = __fadd_rn(acc, __fmul_rn(__uint2float_rn(t[jj]), __ldg(a.invp + u)));
+                else if (u == P) t[jj] = __float2uint_rn(acc);
+            }
+#pragma unroll
+            for (uint32_t pp = 0; pp < kTermsPerChunk / 2; ++pp) {
+                if (16 * pp >= 2 * kl) break;
                 uint32_t h[4];
 #pragma unroll
                 for (int half = 0; half < 2; ++half) {
-                    const uint32_t u = kc * 16 + 2 * pp + half;
-                    uint32_t t = 0;
-                    bool live = true;
-                    if (u < P) {
-                        t = valid ? __ldg(terms + size_t(u) * N + i) : 0u;
-                        acc = __fadd_rn(acc, __fmul_rn(__uint2float_rn(t), __ldg(a.invp + u)));
-                    } else if (u == P) {
-                        t = __float2uint_rn(acc);
-                    } else {
-                        live = false;
-                    }
-                    const uint32_t tb = t + 0x808080u;
+                    const uint32_t u = kc * kTermsPerChunk + 2 * pp + half;
+                    const uint32_t tb = t[2 * pp + half] + 0x808080u;
+                    const bool live = u <= P;
                     h[2 * half] = live ? bytes01_to_half2(tb, kBias128x2) : 0u;
                     h[2 * half + 1] = live ? bytes23_to_half2(tb, kBias128_0) : 0u;
                 }
                 if (!valid) { h[0] = h[1] = h[2] = h[3] = 0; }
-                *reinterpret_cast<uint4*>(tile + kmajor_offset(r, 8 * pp, kl)) = make_uint4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<uint4*>(tileA + kmajor_offset(trow, 8 * pp, kl)) = make_uint4(h[0], h[1], h[2], h[3]);
             }
             fence_proxy_async();
-            mbar_arrive(&ctl->afull[kc & 1]);
+            mbar_arrive(&ctl->afull[s]);
         }
 
         // ---- epilogue.
         if (ok) ok = mbar_wait(&ctl->accfull, 0, abort_flag, a.status);
-        // All threads of the warp execute the TMEM loads (sync.aligned).
-        const uint32_t st = L | 1u;                       // odd staging stride
-        uint32_t* z = zbuf + r * st;
-        int64_t carry = 0;
+        const uint32_t st = L | 1u;                        // odd staging stride
         if (ok) {
             tc_fence_after();
-            const uint32_t taddr = tmem + ((warp * 32) << 16);
-            const uint32_t ncol = a.E;
-            for (uint32_t cb = 0; cb < (ncol + 31) / 32; ++cb) {
-                float v[32];
-                tmem_ld32(taddr + cb * 32, v);
-#pragma unroll
-                for (uint32_t q4 = 0; q4 < 8; ++q4) {
-                    const uint32_t l = cb * 8 + q4;
-                    if (l < L) {
-                        const int64_t s = int64_t(__float2int_rn(v[4 * q4])) +
-                                          (int64_t(__float2int_rn(v[4 * q4 + 1])) << 8) +
-                                          (int64_t(__float2int_rn(v[4 * q4 + 2])) << 16) +
-                                          (int64_t(__float2int_rn(v[4 * q4 + 3])) << 24) + carry;
-                        z[l] = uint32_t(s);
-                        carry = s >> 32;
-                    } else if (l == L && ncol == 4 * L + 1) {
-                        // Extra digit at 256^(4L) = 2^(32L) adds to the top word.
-                        carry += int64_t(__float2int_rn(v[4 * q4]));
-                    }
-                }
-            }
+            const uint32_t taddr = tmem + (((warp & 3) * 32) << 16) + tile * tile_cols;
+            crt_row_epilogue<LT>(a, taddr, zbuf + r * st, valid);
         }
         tc_fence_before();
-        if (ok && valid) {
-            // ---- generic reduction mod q.
-            const uint32_t T = L < 3 ? L : 3;
-            double zhi = double(carry);
-            for (uint32_t t = 0; t < T; ++t) zhi = zhi * 4294967296.0 + double(z[L - 1 - t]);
-            const int64_t k = int64_t(floor(zhi * a.q_inv_scaled));
-            int64_t c = 0;
-            for (uint32_t l = 0; l < L; ++l) {
-                const int64_t s = int64_t(z[l]) - k * int64_t(ctl->q[l]) + c;
-                z[l] = uint32_t(s);
-                c = s >> 32;
-            }
-            const int64_t top = carry + c;
-            if (top < 0) {
-                uint64_t cc = 0;
-                for (uint32_t l = 0; l < L; ++l) {
-                    const uint64_t s = uint64_t(z[l]) + ctl->q[l] + cc;
-                    z[l] = uint32_t(s);
-                    cc = s >> 32;
-                }
-            } else {
-                bool ge = top > 0;
-                if (!ge) {
-                    ge = true;
-                    for (int l = int(L) - 1; l >= 0; --l) {
-                        if (z[l] != ctl->q[l]) { ge = z[l] > ctl->q[l]; break; }
-                    }
-                }
-                if (ge) {
-                    int64_t b = 0;
-                    for (uint32_t l = 0; l < L; ++l) {
-                        const int64_t s = int64_t(z[l]) - int64_t(ctl->q[l]) + b;
-                        z[l] = uint32_t(s);
-                        b = s >> 32;
-                    }
-                }
-            }
-        }
-        // Coalesced store of the staged tile (warps 0-3 only).
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        const uint32_t rows = N - row0 < kTileRows ? N - row0 : kTileRows;
-        for (uint32_t rr = warp; rr < rows; rr += 4) {
+        // Coalesced store of the staged rows (producer warps only).
+        asm volatile("bar.sync 1, %0;" :: "r"(kProdWarps * 32) : "memory");
+        for (uint32_t rr = warp; rr < rows; rr += kProdWarps) {
             uint32_t* dst = out + size_t(row0 + rr) * L;
             const uint32_t* srow = zbuf + rr * st;
             for (uint32_t l = lane; l < L; l += 32) dst[l] = srow[l];
@@ -231,25 +329,36 @@ crt_kernel(CrtArgs a) {
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 4) {
+    if (warp == kProdWarps) {
         tc_fence_after();
-        tmem_dealloc(tmem, kCrtTmemCols);
+        tmem_dealloc(tmem, 2 * tile_cols);
     }
 }
 
 }  // namespace
 
 size_t crt_smem_bytes(uint32_t NC) {
-    return size_t(2) * kTileRows * kCrtChunkK * 2 + size_t(2) * NC * kCrtChunkK * 2 + sizeof(CrtSmem) + 1024;
+    const size_t stage = size_t(kRows) * kCrtChunkK * 2 + size_t(NC) * kCrtChunkK * 2 + kTermsPerChunk * kRows * 4;
+    return kStages * stage + sizeof(CrtSmem) + 1024;
+}
+
+template <int LT>
+static cudaError_t launch_crt_t(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
+    const size_t smem = crt_smem_bytes(a.NC);
+    cudaError_t e = cudaFuncSetAttribute(crt_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    const dim3 grid((a.N + kRows - 1) / kRows, nprod);
+    crt_kernel<LT><<<grid, kCrtThreads, smem, st>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
-    const size_t smem = crt_smem_bytes(a.NC);
-    cudaError_t e = cudaFuncSetAttribute(crt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    const dim3 grid((a.N + kTileRows - 1) / kTileRows, nprod);
-    crt_kernel<<<grid, kCrtThreads, smem, st>>>(a);
-    return cudaGetLastError();
+    switch (a.L) {
+        case 14: return launch_crt_t<14>(a, nprod, st);
+        case 28: return launch_crt_t<28>(a, nprod, st);
+        case 55: return launch_crt_t<55>(a, nprod, st);
+        default: return launch_crt_t<0>(a, nprod, st);
+    }
 }
 
 }  // namespace bcg

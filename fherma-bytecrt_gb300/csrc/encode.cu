@@ -1,8 +1,8 @@
 // RNS encode on the 5th-generation tensor cores (tcgen05, kind::f16).
 //
-// For one tile of 128 coefficients and every prime p_j:
+// For a tile of 128 coefficients and a group of primes p_j:
 //     x_j = sum_k digit_k(coefficient) * (2^(8k+32) mod p_j)
-// as a GEMM [128 x K] x [K x 4P'] where both operands are balanced base-256
+// as a GEMM [128 x K] x [K x 4G] where both operands are balanced base-256
 // digits (|digit| <= 128, exact in fp16) and the 4 output columns of a prime
 // are the 4 balanced digits of 2^(8k+32) mod p_j.  Every digit sum is an
 // integer of magnitude <= K*128*128 < 2^22, exact in the fp32 accumulator.
@@ -15,11 +15,15 @@
 // digits make the fp16 path exact; it replaces the int8 path, whose tensor
 // rate on GB300 is far below the fp16 rate.
 //
-// Warp roles (160 threads): warps 0-3 build the A tile (thread = row) and run
-// the epilogue for their TMEM lane quarter; warp 4 allocates TMEM, streams the
-// B chunks (64 columns = 16 primes) through two shared-memory stages with
-// bulk async copies, and issues the MMAs from one thread.  TMEM holds two
-// 64-column accumulators so the epilogue of chunk c overlaps the MMAs of c+1.
+// Persistent kernel.  The primes are split into NG groups (NG = 2 for P > 16)
+// so that one group's byte-power matrix stays resident in shared memory for
+// the whole launch (one bulk copy per CTA); CTAs of group g loop over all
+// 128-row tiles of all operands and products.  A tiles and TMEM accumulators
+// are double buffered: builders (warps 0-3, thread = row) fill tile i+1 while
+// the MMA of tile i runs and the epilogue warps drain tile i-1.  Warp roles:
+//   warps 0-3    A-tile builders (balanced fp16 digits of one row each)
+//   warps 4-15   epilogue, three warps per TMEM lane quarter, each a third of the columns
+//   warp 16      TMEM allocation, B load, MMA issue (one thread)
 #include "common.cuh"
 #include "kernels.hpp"
 
@@ -27,188 +31,291 @@ namespace bcg {
 namespace {
 
 constexpr uint32_t kTileRows = 128;
-constexpr uint32_t kEncThreads = 160;
-constexpr uint32_t kEncTmemCols = 128;
+constexpr uint32_t kBuildWarps = 4;
+constexpr uint32_t kEpiPerQuarter = 3;
+constexpr uint32_t kEpiWarps = 4 * kEpiPerQuarter;
+constexpr uint32_t kCtlWarp = kBuildWarps + kEpiWarps;
+constexpr uint32_t kEncThreads = (kCtlWarp + 1) * 32;
 
 struct EncodeSmem {
-    uint64_t bfull[2], bempty[2], accfull[2], accempty[2], afull;
+    uint64_t bfull, afull[2], aempty[2], accfull[2], accempty[2], infull[2];
     uint32_t tmem_base;
     uint32_t abort_flag;
 };
 
+// Digits of one coefficient row into the K-major A tile: every input byte b
+// becomes fp16(b - 128) independently (no carries); the digit at k = 4L is
+// the constant 1 that adds back C = 0x80..80 through the B matrix.
+template <int LT>
+__device__ __forceinline__ void digits_row(uint8_t* tile, uint32_t r, const uint32_t* w, uint32_t L, uint32_t K) {
+    const uint32_t words = LT ? uint32_t(LT) : L;
+    uint32_t h[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (uint32_t l = 0; l < (LT ? uint32_t(LT) : 64u); ++l) {
+        if (!LT && l >= words) break;
+        h[2 * (l & 1)] = bytes01_to_half2(w[l], kBias128x2);
+        h[2 * (l & 1) + 1] = bytes23_to_half2(w[l], kBias128x2);
+        if (l & 1)
+            *reinterpret_cast<uint4*>(tile + kmajor_offset(r, 8 * (l >> 1), K)) = make_uint4(h[0], h[1], h[2], h[3]);
+    }
+    // Tail: the constant digit right after the last word, then zero padding.
+    uint32_t kc = words / 2;
+    if (words & 1) {
+        h[2] = 0x00003C00u;                       // fp16 1.0 at k = 4L
+        h[3] = 0;
+    } else {
+        h[0] = 0x00003C00u;
+        h[1] = h[2] = h[3] = 0;
+    }
+    *reinterpret_cast<uint4*>(tile + kmajor_offset(r, 8 * kc, K)) = make_uint4(h[0], h[1], h[2], h[3]);
+    for (++kc; kc < K / 8; ++kc)
+        *reinterpret_cast<uint4*>(tile + kmajor_offset(r, 8 * kc, K)) = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// x = sum_d S_d 256^d from four exact fp32 digit sums, then (x - m p) / 2^32.
+// With |S_d| < 2^22: u = S_3*256 + S_2 and v = S_1*256 + S_0 fit int32 and
+// x = u * 2^16 + v is one wide multiply-add.  The signed Montgomery quotient
+// t = hi(x) - hi(m p) lies in (-p - 2^14, 2^14]; min(t + p, t + 2p) taken as
+// unsigned picks the representative in [0, 2p).
+__device__ __forceinline__ uint32_t encode_residue(float s0, float s1, float s2, float s3, uint2 pc) {
+    // Bit patterns of S + 1.5*2^23 carry S + 0x4B400000; wrapping unsigned
+    // arithmetic removes the bias exactly (the true u and v fit int32).
+    const uint32_t b0 = __float_as_uint(s0 + 12582912.0f), b1 = __float_as_uint(s1 + 12582912.0f);
+    const uint32_t b2 = __float_as_uint(s2 + 12582912.0f), b3 = __float_as_uint(s3 + 12582912.0f);
+    constexpr uint32_t kBias257 = 0x4B400000u * 257u;
+    const int32_t u = int32_t(b3 * 256u + b2 - kBias257);
+    const int32_t v = int32_t(b1 * 256u + b0 - kBias257);
+    const int64_t x = int64_t(u) * 65536 + v;
+    const uint32_t m = uint32_t(x) * pc.y;
+    const uint32_t t = uint32_t(int32_t(x >> 32)) - __umulhi(m, pc.x);
+    return min(t + pc.x, t + 2 * pc.x);
+}
+
+template <int LT>
 __global__ void __launch_bounds__(kEncThreads, 1)
-encode_kernel(EncodeArgs a) {
+encode_kernel(const __grid_constant__ EncodeArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    const uint32_t K = a.K;
-    uint8_t* tileA = smem;                                           // 128 x K fp16
-    uint8_t* stageB = smem + kTileRows * K * 2;                      // 2 x 64 x K fp16
-    EncodeSmem* ctl = reinterpret_cast<EncodeSmem*>(stageB + 2 * kEncChunkCols * K * 2);
+    const uint32_t K = a.K, L = LT ? uint32_t(LT) : a.L;
+    const uint32_t ng = a.groups;
+    const uint32_t g = blockIdx.x % ng;                       // prime group of this CTA
+    const uint32_t slot = blockIdx.x / ng, nslots = gridDim.x / ng;
+    const uint32_t col0 = g * a.group_cols;                   // first B column of the group
+    const uint32_t gcols = min(a.group_cols, a.cols - col0);  // multiple of 16
+    const uint32_t tile_bytes = kTileRows * K * 2;
+    uint8_t* tiles = smem;                                    // 2 x tile_bytes
+    uint8_t* bres = smem + 2 * tile_bytes;                    // gcols x K fp16, resident
+    EncodeSmem* ctl = reinterpret_cast<EncodeSmem*>(bres + a.group_cols * K * 2);
     volatile uint32_t* abort_flag = &ctl->abort_flag;
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t operand = blockIdx.y, prod = blockIdx.z;
-    const uint32_t row0 = blockIdx.x * kTileRows;
-    const uint32_t* in = (operand ? a.in1 : a.in0) + size_t(prod) * a.in_stride;
-    uint32_t* planes = (operand ? a.out1 : a.out0) + size_t(prod) * a.out_stride;
+    const uint32_t ntiles = (a.N + kTileRows - 1) / kTileRows;
+    const uint32_t njobs = a.nprod * a.operands * ntiles;
 
     if (threadIdx.x == 0) {
+        mbar_init(&ctl->bfull, 1);
         for (int i = 0; i < 2; ++i) {
-            mbar_init(&ctl->bfull[i], 1);
-            mbar_init(&ctl->bempty[i], 1);
+            mbar_init(&ctl->afull[i], kTileRows);
+            mbar_init(&ctl->aempty[i], 1);
             mbar_init(&ctl->accfull[i], 1);
-            mbar_init(&ctl->accempty[i], kTileRows);
+            mbar_init(&ctl->accempty[i], kEpiWarps * 32);
+            mbar_init(&ctl->infull[i], 1);
         }
-        mbar_init(&ctl->afull, kTileRows);
         ctl->abort_flag = 0;
         mbar_fence_init();
     }
-    if (warp == 4) {
-        tmem_alloc(&ctl->tmem_base, kEncTmemCols);
+    if (warp == kCtlWarp) {
+        tmem_alloc(&ctl->tmem_base, 512);
         tmem_relinquish();
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = ctl->tmem_base;
-    const uint32_t nchunks = a.chunks;
 
-    if (warp == 4) {
+    if (warp == kCtlWarp) {
         if (lane == 0) {
-            auto chunk_cols = [&](uint32_t c) { return min(kEncChunkCols, a.cols - c * kEncChunkCols); };
-            auto load_chunk = [&](uint32_t c) {
-                const uint32_t bytes = chunk_cols(c) * K * 2;
-                mbar_arrive_expect_tx(&ctl->bfull[c & 1], bytes);
-                bulk_load(stageB + (c & 1) * kEncChunkCols * K * 2,
-                          a.enc_b + size_t(c) * kEncChunkCols * K, bytes, &ctl->bfull[c & 1]);
-            };
-            load_chunk(0);
-            if (nchunks > 1) load_chunk(1);
-            bool ok = mbar_wait(&ctl->afull, 0, abort_flag, a.status);
-            for (uint32_t c = 0; ok && c < nchunks; ++c) {
-                if (c >= 2) ok = mbar_wait(&ctl->accempty[c & 1], ((c >> 1) - 1) & 1, abort_flag, a.status);
-                if (ok) ok = mbar_wait(&ctl->bfull[c & 1], (c >> 1) & 1, abort_flag, a.status);
+            // The group's columns are one contiguous K-major range (8-row groups are contiguous).
+            const uint32_t bbytes = gcols * K * 2;
+            mbar_arrive_expect_tx(&ctl->bfull, bbytes);
+            bulk_load(bres, a.enc_b + size_t(col0) * K, bbytes, &ctl->bfull);
+            bool ok = mbar_wait(&ctl->bfull, 0, abort_flag, a.status);
+            const uint32_t sbo = (K / 8) * 128;
+            const uint32_t idesc = idesc_f16_f32(kTileRows, gcols);
+            const uint32_t b_addr = smem_u32(bres);
+            uint32_t ii = 0;
+            for (uint32_t job = slot; ok && job < njobs; job += nslots, ++ii) {
+                const uint32_t s = ii & 1, use = ii >> 1;
+                ok = mbar_wait(&ctl->afull[s], use & 1, abort_flag, a.status);
+                if (ok && ii >= 2) ok = mbar_wait(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t n = chunk_cols(c);
-                const uint32_t idesc = idesc_f16_f32(kTileRows, n);
-                const uint32_t a_addr = smem_u32(tileA);
-                const uint32_t b_addr = smem_u32(stageB + (c & 1) * kEncChunkCols * K * 2);
-                const uint32_t sbo = (K / 8) * 128;
-                for (uint32_t ks = 0; ks < K / 16; ++ks) {
-                    const uint64_t ad = smem_desc(a_addr + ks * 256, 128, sbo);
-                    const uint64_t bd = smem_desc(b_addr + ks * 256, 128, sbo);
-                    mma_f16(tmem + (c & 1) * 64, ad, bd, idesc, ks > 0);
-                }
-                mma_commit(&ctl->accfull[c & 1]);
-                mma_commit(&ctl->bempty[c & 1]);
-                if (c >= 1 && c + 1 < nchunks) {
-                    // Stage of chunk c-1 is free once its MMAs retired; refill with c+1.
-                    ok = mbar_wait(&ctl->bempty[(c - 1) & 1], ((c - 1) >> 1) & 1, abort_flag, a.status);
-                    if (ok) load_chunk(c + 1);
-                }
+                const uint32_t a_addr = smem_u32(tiles + s * tile_bytes);
+                for (uint32_t ks = 0; ks < K / 16; ++ks)
+                    mma_f16(tmem + s * 256, smem_desc(a_addr + ks * 256, 128, sbo),
+                            smem_desc(b_addr + ks * 256, 128, sbo), idesc, ks > 0);
+                mma_commit(&ctl->accfull[s]);
+                mma_commit(&ctl->aempty[s]);
             }
-            // Drain: the last commits must land before TMEM is freed.
-            if (nchunks >= 1) mbar_wait(&ctl->bempty[(nchunks - 1) & 1], ((nchunks - 1) >> 1) & 1, abort_flag, a.status);
-            if (nchunks >= 2) mbar_wait(&ctl->bempty[(nchunks - 2) & 1], ((nchunks - 2) >> 1) & 1, abort_flag, a.status);
+            // Drain the last commits before TMEM is freed.
+            for (uint32_t back = 1; back <= 2 && back <= ii; ++back) {
+                const uint32_t jj = ii - back;
+                mbar_wait(&ctl->aempty[jj & 1], (jj >> 1) & 1, abort_flag, a.status);
+            }
         }
         __syncwarp();
-    } else {
-        // ---- A tile: balanced digits of this thread's coefficient row.
-        const uint32_t r = threadIdx.x;                 // 0..127
-        const uint32_t i = row0 + r;
-        const bool valid = i < a.N;
-        const uint32_t* src = in + size_t(i) * a.L;
-        uint32_t carry = 0;
-        const uint32_t L = a.L;
-        for (uint32_t kc = 0; kc < K / 8; ++kc) {       // 8 digits = 2 input words per store
-            uint32_t h[4];
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const uint32_t l = 2 * kc + half;
-                uint32_t lo0 = 0, lo1 = 0;
-                if (l < L) {
-                    const uint32_t w = valid ? __ldg(src + l) : 0u;
-                    const uint64_t s = uint64_t(w) + 0x80808080u + carry;
-                    const uint32_t v = uint32_t(s);
-                    carry = uint32_t(s >> 32);
-                    lo0 = bytes01_to_half2(v, kBias128x2);
-                    lo1 = bytes23_to_half2(v, kBias128x2);
-                } else if (l == L && valid && carry) {
-                    lo0 = 0x00003C00u;      // fp16 1.0 in the low half: the carry digit
-                    carry = 0;
+    } else if (warp < kBuildWarps) {
+        // ---- builders: thread = row of the tile.  The tile's input rows are
+        // contiguous: one bulk copy stages them in the tail of the A buffer
+        // being filled; every builder reads its row before any digit is
+        // written (named barrier), so the in-place conversion is race free.
+        const uint32_t r = threadIdx.x;
+        const uint32_t stage_off = (tile_bytes - kTileRows * L * 4) & ~15u;
+        uint32_t ii = 0;
+        for (uint32_t job = slot; job < njobs; job += nslots, ++ii) {
+            const uint32_t s = ii & 1, use = ii >> 1;
+            if (ii >= 2 && !mbar_wait(&ctl->aempty[s], (use - 1) & 1, abort_flag, a.status)) break;
+            const uint32_t tile = job % ntiles, operand = (job / ntiles) % a.operands;
+            const uint32_t prod = job / (ntiles * a.operands);
+            const uint32_t rows = min(kTileRows, a.N - tile * kTileRows);
+            uint8_t* buf = tiles + s * tile_bytes;
+            const uint32_t* staged = reinterpret_cast<const uint32_t*>(buf + stage_off);
+            if (r == 0) {
+                // Warm L2 with the input of the job after next.
+                const uint32_t pj = job + 2 * nslots;
+                if (pj < njobs) {
+                    const uint32_t pt = pj % ntiles, po = (pj / ntiles) % a.operands, pp = pj / (ntiles * a.operands);
+                    const uint32_t prow = min(kTileRows, a.N - pt * kTileRows);
+                    bulk_prefetch_l2((po ? a.in1 : a.in0) + size_t(pp) * a.in_stride + size_t(pt) * kTileRows * L,
+                                     prow * L * 4);
                 }
-                h[2 * half] = lo0;
-                h[2 * half + 1] = lo1;
+                const uint32_t bytes = rows * L * 4;
+                mbar_arrive_expect_tx(&ctl->infull[s], bytes);
+                bulk_load(buf + stage_off,
+                          (operand ? a.in1 : a.in0) + size_t(prod) * a.in_stride + size_t(tile) * kTileRows * L,
+                          bytes, &ctl->infull[s]);
             }
-            if (!valid) { h[0] = h[1] = h[2] = h[3] = 0; }
-            *reinterpret_cast<uint4*>(tileA + kmajor_offset(r, 8 * kc, K)) = make_uint4(h[0], h[1], h[2], h[3]);
+            const bool valid = r < rows;
+            const bool ok_in = mbar_wait(&ctl->infull[s], use & 1, abort_flag, a.status);
+            uint32_t w[LT ? LT : 64];
+#pragma unroll
+            for (uint32_t l = 0; l < (LT ? uint32_t(LT) : 64u); ++l) {
+                if (!LT && l >= L) break;
+                w[l] = (valid && ok_in) ? staged[r * L + l] : 0u;
+            }
+            asm volatile("bar.sync 1, %0;" :: "r"(kBuildWarps * 32) : "memory");
+            if (!ok_in) break;
+            if (valid) {
+                digits_row<LT>(buf, r, w, L, K);
+            } else {
+                for (uint32_t kc = 0; kc < K / 8; ++kc)
+                    *reinterpret_cast<uint4*>(buf + kmajor_offset(r, 8 * kc, K)) = make_uint4(0u, 0u, 0u, 0u);
+            }
+            fence_proxy_async();
+            mbar_arrive(&ctl->afull[s]);
         }
-        fence_proxy_async();
-        mbar_arrive(&ctl->afull);
-
-        // ---- Epilogue: residues for this thread's row, chunk by chunk.
-        const uint32_t quarter = warp;                  // TMEM lanes 32*warp .. +31
-        for (uint32_t c = 0; c < nchunks; ++c) {
-            if (!mbar_wait(&ctl->accfull[c & 1], (c >> 1) & 1, abort_flag, a.status)) break;
+    } else {
+        // ---- epilogue: quarter of TMEM lanes, a third of the group's primes.
+        const uint32_t e = warp - kBuildWarps;
+        const uint32_t quarter = e & 3, part = e >> 2;        // part 0..2
+        const uint32_t r = quarter * 32 + lane;
+        const uint32_t gp = gcols / 4;                        // primes in this group (incl. padding)
+        const uint32_t per = (gp + kEpiPerQuarter - 1) / kEpiPerQuarter;
+        const uint32_t p0 = part * per, p1 = min(gp, p0 + per);
+        uint32_t ii = 0;
+        for (uint32_t job = slot; job < njobs; job += nslots, ++ii) {
+            const uint32_t s = ii & 1, use = ii >> 1;
+            if (!mbar_wait(&ctl->accfull[s], use & 1, abort_flag, a.status)) break;
             tc_fence_after();
-            const uint32_t n = min(kEncChunkCols, a.cols - c * kEncChunkCols);
-            float v[64];
-            {
-                float t0[32];
-                tmem_ld32(tmem + ((quarter * 32) << 16) + (c & 1) * 64, t0);
+            const uint32_t tile = job % ntiles, operand = (job / ntiles) % a.operands;
+            const uint32_t prod = job / (ntiles * a.operands);
+            const uint32_t i = tile * kTileRows + r;
+            const bool valid = i < a.N;
+            uint32_t* planes = (operand ? a.out1 : a.out0) + size_t(prod) * a.out_stride;
+            const uint32_t taddr = tmem + ((quarter * 32) << 16) + s * 256;
+            // Up to 24 primes (96 columns) per warp, 32 columns (8 primes) at a time.
+#pragma unroll 1
+            for (uint32_t cb = 0; cb < 3; ++cb) {
+                if (cb * 8 >= p1 - p0) break;                       // warp-uniform
+                float v[32];
+                tmem_ld32(taddr + 4 * p0 + cb * 32, v);
+                if (valid) {
 #pragma unroll
-                for (int q = 0; q < 32; ++q) v[q] = t0[q];
-                if (n > 32) {
-                    tmem_ld32(tmem + ((quarter * 32) << 16) + (c & 1) * 64 + 32, t0);
-#pragma unroll
-                    for (int q = 0; q < 32; ++q) v[32 + q] = t0[q];
+                    for (uint32_t jj = 0; jj < 8; ++jj) {
+                        const uint32_t lp = p0 + cb * 8 + jj;                 // prime within the group
+                        const uint32_t j = g * (a.group_cols / 4) + lp;        // global prime
+                        if (lp < p1 && j < a.P)
+                            planes[size_t(j) * a.N + i] =
+                                encode_residue(v[4 * jj], v[4 * jj + 1], v[4 * jj + 2], v[4 * jj + 3], a.prime[j]);
+                    }
                 }
             }
             tc_fence_before();
-            mbar_arrive(&ctl->accempty[c & 1]);
-            if (valid) {
-#pragma unroll
-                for (uint32_t jj = 0; jj < 16; ++jj) {
-                    if (4 * jj >= n) break;
-                    const uint32_t j = c * 16 + jj;
-                    if (j >= a.P) break;
-                    const uint4 pc = __ldg(a.consts + j);
-                    const int32_t y0 = small_float_to_int(v[4 * jj]);
-                    const int32_t y1 = small_float_to_int(v[4 * jj + 1]);
-                    const int32_t y2 = small_float_to_int(v[4 * jj + 2]);
-                    const int32_t y3 = small_float_to_int(v[4 * jj + 3]);
-                    const int64_t x = int64_t(y0) + (int64_t(y1) << 8) + (int64_t(y2) << 16) + (int64_t(y3) << 24);
-                    // Signed Montgomery: (x - m p) / 2^32 with m = x * p^-1 mod 2^32.
-                    const uint32_t m = uint32_t(x) * pc.y;
-                    const int32_t t = int32_t(x >> 32) - int32_t(__umulhi(m, pc.x));
-                    int32_t res = t + int32_t(pc.x);
-                    res = res < 0 ? res + int32_t(pc.x) : res;
-                    planes[size_t(j) * a.N + i] = uint32_t(res);
-                }
-            }
+            mbar_arrive(&ctl->accempty[s]);
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 4) {
+    if (warp == kCtlWarp) {
         tc_fence_after();
-        tmem_dealloc(tmem, kEncTmemCols);
+        tmem_dealloc(tmem, 512);
     }
 }
 
 }  // namespace
 
-size_t encode_smem_bytes(uint32_t K) {
-    return size_t(kTileRows) * K * 2 + size_t(2) * kEncChunkCols * K * 2 + sizeof(EncodeSmem) + 1024;
+// Column groups: the resident B of one group plus two A tiles must fit the
+// 227 KB of shared memory; each group is at most 256 columns (one MMA).
+uint32_t encode_group_cols(uint32_t cols, uint32_t K) {
+    const uint32_t budget = 227 * 1024 - 2 * kTileRows * K * 2 - 1024 - sizeof(EncodeSmem);
+    uint32_t groups = 1;
+    while (true) {
+        const uint32_t gc = ((cols + groups - 1) / groups + 15) / 16 * 16;
+        if (gc <= 240 && gc * K * 2 <= budget) return gc;
+        ++groups;
+    }
 }
 
-cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands) {
-    const size_t smem = encode_smem_bytes(a.K);
-    cudaError_t e = cudaFuncSetAttribute(encode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+size_t encode_smem_bytes(uint32_t K, uint32_t group_cols) {
+    return size_t(2) * kTileRows * K * 2 + size_t(group_cols) * K * 2 + sizeof(EncodeSmem) + 1024;
+}
+
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int LT>
+static cudaError_t launch_encode_t(EncodeArgs a, uint32_t nprod, cudaStream_t st, uint32_t operands) {
+    a.group_cols = encode_group_cols(a.cols, a.K);
+    a.groups = (a.cols + a.group_cols - 1) / a.group_cols;
+    a.nprod = nprod;
+    a.operands = operands;
+    const size_t smem = encode_smem_bytes(a.K, a.group_cols);
+    cudaError_t e = cudaFuncSetAttribute(encode_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    const dim3 grid((a.N + kTileRows - 1) / kTileRows, operands, nprod);
-    encode_kernel<<<grid, kEncThreads, smem, st>>>(a);
+    const uint32_t ntiles = (a.N + kTileRows - 1) / kTileRows;
+    const uint32_t jobs = nprod * operands * ntiles;
+    uint32_t slots = uint32_t(sm_count()) / a.groups;
+    if (slots < 1) slots = 1;
+    if (slots > jobs) slots = jobs;
+    encode_kernel<LT><<<slots * a.groups, kEncThreads, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands,
+                          const EncodeTuning&) {
+    switch (a.L) {
+        case 14: return launch_encode_t<14>(a, nprod, st, operands);
+        case 28: return launch_encode_t<28>(a, nprod, st, operands);
+        case 55: return launch_encode_t<55>(a, nprod, st, operands);
+        default: return launch_encode_t<0>(a, nprod, st, operands);
+    }
 }
 
 }  // namespace bcg

@@ -65,13 +65,14 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     ntt_.N = g.N; ntt_.P = g.P; ntt_.c_bits = g.c_bits; ntt_.z_bits = g.z_bits; ntt_.Z = g.Z; ntt_.H = g.H;
 
     enc_.enc_b = enc_b_.as<uint16_t>();
-    enc_.consts = consts_.as<uint4>();
+    for (uint32_t j = 0; j < g.P; ++j)
+        enc_.prime[j] = make_uint2(plan_.prime_consts[4 * j], plan_.prime_consts[4 * j + 1]);
     enc_.N = g.N; enc_.L = g.L; enc_.P = g.P; enc_.K = g.enc_k; enc_.cols = g.enc_cols; enc_.chunks = g.enc_chunks;
     enc_.status = status_.as<uint32_t>();
 
     crt_.crt_b = crt_b_.as<uint16_t>();
     crt_.invp = invp_.as<float>();
-    crt_.q = q_.as<uint32_t>();
+    for (uint32_t l = 0; l < g.L; ++l) crt_.q[l] = plan_.q[l];
     crt_.q_inv_scaled = plan_.q_inv_scaled;
     crt_.N = g.N; crt_.L = g.L; crt_.P = g.P; crt_.k_total = g.crt_k_total; crt_.kchunks = g.crt_kchunks;
     crt_.E = g.crt_e; crt_.NC = g.crt_n;
@@ -103,25 +104,62 @@ void Context::ensure_workspace(uint32_t products) {
     ws_products_ = products;
 }
 
-void Context::ensure_host_staging(uint32_t products) {
-    if (products <= io_products_) return;
+void Context::ensure_device_io(uint32_t products) {
+    if (products <= io_dev_products_) return;
     cudaStreamSynchronize(stream_);
     cudaStreamSynchronize(copy_in_);
     cudaStreamSynchronize(copy_out_);
     const size_t bytes = size_t(products) * coeff_words() * 4 * 3;
-    for (int s = 0; s < 2; ++s) {
-        io_dev_[s].allocate(bytes);
-        io_host_[s].allocate(bytes);
-    }
+    for (int s = 0; s < 2; ++s) io_dev_[s].allocate(bytes);
+    io_dev_products_ = products;
+}
+
+void Context::ensure_host_staging(uint32_t products) {
+    ensure_device_io(products);
+    if (products <= io_products_) return;
+    const size_t bytes = size_t(products) * coeff_words() * 4 * 3;
+    for (int s = 0; s < 2; ++s) io_host_[s].allocate(bytes);
     io_products_ = products;
+}
+
+// Host buffers that are already pinned: DMA straight from and to them, with
+// two device slots so the copies of one group overlap the compute of the other.
+void Context::multiply_pinned(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count) {
+    const uint32_t g = std::min(group_, count);
+    ensure_workspace(g);
+    ensure_device_io(g);
+    const size_t cw = coeff_words();
+    const uint32_t ngroups = (count + g - 1) / g;
+    for (uint32_t gi = 0; gi < ngroups; ++gi) {
+        const int s = gi & 1;
+        const uint32_t n = std::min(g, count - gi * g);
+        const size_t off = size_t(gi) * g * cw, bytes = size_t(n) * cw * 4;
+        uint32_t* d = io_dev_[s].as<uint32_t>();
+        if (gi >= 2) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
+        check(cudaMemcpyAsync(d, a + off, bytes, cudaMemcpyHostToDevice, copy_in_), "input copy");
+        check(cudaMemcpyAsync(d + g * cw, b + off, bytes, cudaMemcpyHostToDevice, copy_in_), "input copy");
+        check(cudaEventRecord(ev_in_[s], copy_in_), "event");
+        check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
+        if (gi >= 2) check(cudaStreamWaitEvent(stream_, ev_out_[s], 0), "slot reuse");
+        chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_);
+        check(cudaEventRecord(ev_done_[s], stream_), "event");
+        check(cudaStreamWaitEvent(copy_out_, ev_done_[s], 0), "event wait");
+        check(cudaMemcpyAsync(c + off, d + 2 * g * cw, bytes, cudaMemcpyDeviceToHost, copy_out_), "output copy");
+        check(cudaEventRecord(ev_out_[s], copy_out_), "event");
+    }
+    check(cudaStreamSynchronize(copy_out_), "output copy");
+    check_status();
 }
 
 void Context::encode(const uint32_t* a, const uint32_t* b, uint32_t* pa, uint32_t* pb, size_t plane_stride,
                      uint32_t count, cudaStream_t st) {
+    // The encode kernel bulk-copies input tiles: their addresses must be 16-byte aligned.
+    if ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15)
+        throw std::invalid_argument("operand device pointers must be 16-byte aligned");
     EncodeArgs e = enc_;
     e.in0 = a; e.in1 = b; e.in_stride = coeff_words();
     e.out0 = pa; e.out1 = pb; e.out_stride = plane_stride;
-    check(launch_encode(e, count, st), "encode launch");
+    check(launch_encode(e, count, st, 2, enc_tuning_), "encode launch");
 }
 
 void Context::negacyclic(uint32_t* pa, uint32_t* pb, size_t plane_stride, uint32_t count, cudaStream_t st) {
@@ -215,7 +253,7 @@ void Context::forward_spectral(const uint32_t* x, uint32_t* planes, cudaStream_t
     EncodeArgs e = enc_;
     e.in0 = x; e.in1 = x; e.in_stride = 0;
     e.out0 = planes; e.out1 = planes; e.out_stride = 0;
-    check(launch_encode(e, 1, st, 1), "encode launch");
+    check(launch_encode(e, 1, st, 1, enc_tuning_), "encode launch");
     check(launch_col_forward(ntt_, planes, 0, 1, st), "column pass launch");
     check(launch_row_forward(ntt_, planes, 0, 1, st), "row forward launch");
 }
@@ -226,7 +264,7 @@ void Context::multiply_spectral_device(const uint32_t* a_spectral, const uint32_
     EncodeArgs e = enc_;
     e.in0 = b; e.in1 = b; e.in_stride = coeff_words();
     e.out0 = ws; e.out1 = ws; e.out_stride = pw;
-    check(launch_encode(e, count, st, 1), "encode launch");
+    check(launch_encode(e, count, st, 1, enc_tuning_), "encode launch");
     check(launch_col_forward(ntt_, ws, pw, count, st), "column pass launch");
     check(launch_row_product(ntt_, a_spectral, 0, ws, pw, ws, pw, count, true, st), "row pass launch");
     check(launch_col_inverse(ntt_, ws, pw, count, st), "inverse column pass launch");

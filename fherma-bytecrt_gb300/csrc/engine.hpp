@@ -102,6 +102,8 @@ public:
     void chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, uint32_t* ws, cudaStream_t st);
 
     NttArgs ntt_args() const { return ntt_; }
+    EncodeTuning& encode_tuning() { return enc_tuning_; }
+    const EncodeTuning& encode_tuning() const { return enc_tuning_; }
 
     // Per-stage timing with CUDA events recorded on the launching stream.
     enum Stage { kEncode = 0, kColForward, kRow, kColInverse, kCrt, kStages };
@@ -121,7 +123,9 @@ private:
     uint64_t launches_total_ = 0, chains_ = 0;
 
     void ensure_workspace(uint32_t products);
+    void ensure_device_io(uint32_t products);
     void ensure_host_staging(uint32_t products);
+    void multiply_pinned(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
 
     HostPlan plan_;
     int device_ = 0;
@@ -134,11 +138,12 @@ private:
     // Host-buffer path: double-buffered device inputs/outputs and pinned staging.
     DeviceBuffer io_dev_[2];
     PinnedBuffer io_host_[2];
-    size_t io_products_ = 0;
+    size_t io_products_ = 0, io_dev_products_ = 0;
     cudaEvent_t ev_in_[2] = {}, ev_done_[2] = {}, ev_out_[2] = {};
     NttArgs ntt_{};
     EncodeArgs enc_{};
     CrtArgs crt_{};
+    EncodeTuning enc_tuning_{};
 };
 
 // Thread-local last error message for the C ABI.

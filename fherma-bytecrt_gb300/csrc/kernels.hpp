@@ -9,6 +9,11 @@
 
 namespace bcg {
 
+constexpr uint32_t kMaxPrimes = 256;
+constexpr uint32_t kMaxLimbs = 64;
+
+// Kernel arguments are passed by value; the small per-point constants ride in
+// the parameter space (constant bank), where warp-uniform reads are free.
 struct EncodeArgs {
     const uint32_t* in0;     // operand A coefficients [N][L] (product z at + z*in_stride)
     const uint32_t* in1;     // operand B
@@ -17,9 +22,10 @@ struct EncodeArgs {
     uint32_t* out1;
     size_t out_stride;
     const uint16_t* enc_b;   // fp16 byte-power matrix, chunked
-    const uint4* consts;     // per prime: p, p^-1, -p^-1, 0
     uint32_t N, L, P, K, cols, chunks;
     uint32_t* status;
+    uint32_t groups, group_cols, nprod, operands;   // set by the launcher
+    uint2 prime[kMaxPrimes]; // p, p^-1 mod 2^32
 };
 
 struct CrtArgs {
@@ -29,19 +35,27 @@ struct CrtArgs {
     size_t out_stride;
     const uint16_t* crt_b;   // fp16 weight-digit matrix, chunked over K
     const float* invp;
-    const uint32_t* q;
     double q_inv_scaled;
     uint32_t N, L, P, k_total, kchunks, E, NC;
     uint32_t* status;
+    uint32_t q[kMaxLimbs];
 };
 
 struct NttArgs;   // ntt.cuh
 
-size_t encode_smem_bytes(uint32_t K);
+// Encode pipeline knobs: B-operand stages (2 or 3) and TMEM chunk buffers (2 or 4).
+struct EncodeTuning {
+    uint32_t bstages = 2;
+    uint32_t accbuf = 4;
+};
+
+size_t encode_smem_bytes(uint32_t K, uint32_t group_cols);
+uint32_t encode_group_cols(uint32_t cols, uint32_t K);
 size_t crt_smem_bytes(uint32_t NC);
 
 // Encodes operand A (and operand B when operands == 2) of nprod products (grid.y = operand).
-cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands = 2);
+cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands = 2,
+                          const EncodeTuning& tuning = EncodeTuning());
 cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st);
 
 // Column passes over nplanes prime-plane sets, set z at planes + z*stride.

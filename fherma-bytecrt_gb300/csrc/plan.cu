@@ -250,10 +250,12 @@ HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw) {
         if (!(g.P * gamma < 0.2)) throw std::invalid_argument("fp32 alpha bound fails for this prime count");
     }
 
-    // Encode GEMM shape.  A coefficient below q < 2^W gets a carry digit only
-    // when W > 32L - 2 (then x + 0x80..80 can reach 2^(32L)).
+    // Encode GEMM shape: the 4L input bytes enter as b - 128 (no carries), and
+    // one extra K row with A digit 1 adds back C = 0x80..80 (4L bytes).
+    g.enc_k_real = 4 * L + 1;
+    // The CRT output digits of a weight below q < 2^W need a carry digit only
+    // when W > 32L - 2 (then w + 0x80..80 can reach 2^(32L)).
     const uint32_t extra = W > 32 * L - 2 ? 1 : 0;
-    g.enc_k_real = 4 * L + extra;
     g.enc_k = (g.enc_k_real + 15) / 16 * 16;
     if (g.enc_k_real > 256) throw std::invalid_argument("encode digit sums exceed the fp32 exact range");
     const uint32_t p4 = (g.P + 3) / 4 * 4;
@@ -344,7 +346,8 @@ HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw) {
     }
 
     // Encode B: chunk c holds columns [64c, 64c + cols_c) in K-major core-matrix
-    // order over K = enc_k.  Column n = 4*j + d: digit d of 2^(8k+32) mod p_j.
+    // order over K = enc_k.  Column n = 4*j + d: digit d of 2^(8k+32) mod p_j for
+    // k < 4L, and at k = 4L digit d of C * 2^32 mod p_j with C = sum_k 128 * 256^k.
     plan.enc_b.assign(size_t(g.enc_cols) * g.enc_k, 0);
     for (uint32_t col = 0; col < g.enc_cols; ++col) {
         const uint32_t j = col / 4, d = col % 4;
@@ -353,12 +356,17 @@ HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw) {
         const uint32_t chunk = col / kEncChunkCols, n = col % kEncChunkCols;
         uint16_t* dst = plan.enc_b.data() + size_t(chunk) * kEncChunkCols * g.enc_k;
         uint32_t w = pow_mod(2, 32, pj);
-        for (uint32_t k = 0; k < g.enc_k_real; ++k) {
+        uint64_t cterm = 0;                          // C * 2^32 mod p_j
+        for (uint32_t k = 0; k < 4 * L; ++k) {
             int dg[4];
             digits31(w, dg);
             dst[kmajor_offset(n, k, g.enc_k) / 2] = half_bits(dg[d]);
+            cterm = (cterm + 128ull * w) % pj;
             w = uint32_t(uint64_t(w) * 256 % pj);
         }
+        int dg[4];
+        digits31(uint32_t(cterm), dg);
+        dst[kmajor_offset(n, 4 * L, g.enc_k) / 2] = half_bits(dg[d]);
     }
 
     // CRT B: K chunk kc holds k = 4u + a for terms u in [16kc, 16kc + 16), rows

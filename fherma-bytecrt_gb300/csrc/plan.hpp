@@ -28,7 +28,7 @@ struct Geometry {
 };
 
 constexpr uint32_t kEncChunkCols = 64;   // 16 primes x 4 digits per MMA chunk
-constexpr uint32_t kCrtChunkK = 64;      // 16 terms x 4 digits per K chunk
+constexpr uint32_t kCrtChunkK = 32;      // 8 terms x 4 digits per K chunk
 
 struct HostPlan {
     Geometry g;

@@ -70,6 +70,9 @@ def lib():
         L.bcg_context_destroy.argtypes = [vp]
         L.bcg_context_destroy.restype = None
         L.bcg_context_info.argtypes = [vp, ctypes.POINTER(bcg_info)]
+        L.bcg_context_set_group.argtypes = [vp, ctypes.c_uint32]
+        L.bcg_context_set_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
+        L.bcg_context_get_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.bcg_multiply.argtypes = [vp, _u32p, _u32p, _u32p, ctypes.c_uint32]
         L.bcg_multiply_device.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
         L.bcg_encode_device.argtypes = [vp, vp, vp, vp, vp, ctypes.c_size_t, ctypes.c_uint32, vp]
@@ -160,6 +163,23 @@ class Multiplier:
     @property
     def plane_words(self) -> int:
         return self.P * self.N
+
+    def set_group(self, group: int):
+        _check(lib().bcg_context_set_group(self._h, int(group)))
+        info = bcg_info()
+        _check(lib().bcg_context_info(self._h, ctypes.byref(info)))
+        self.info = info
+
+    def set_tuning(self, knob: str, value: int):
+        _check(lib().bcg_context_set_tuning(self._h, knob.encode(), int(value)))
+        info = bcg_info()
+        _check(lib().bcg_context_info(self._h, ctypes.byref(info)))
+        self.info = info
+
+    def get_tuning(self, knob: str) -> int:
+        v = ctypes.c_int64()
+        _check(lib().bcg_context_get_tuning(self._h, knob.encode(), ctypes.byref(v)))
+        return int(v.value)
 
     # ---- host buffers
     def multiply(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:

@@ -68,6 +68,15 @@ int bcg_plan_weights(const bcg_plan* plan, uint32_t* weights);
 int bcg_context_create(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int device, bcg_context** out);
 void bcg_context_destroy(bcg_context* ctx);
 int bcg_context_info(const bcg_context* ctx, bcg_info* out);
+/* Products per launch chain (grid.z of every stage).  The default fills the
+ * GPU for the point; the autotuner may change it. */
+int bcg_context_set_group(bcg_context* ctx, uint32_t group);
+/* Kernel shape knobs (the autotuner's search space), by name:
+ *   "group"           products per launch chain, 1..4096
+ *   "encode_bstages"  B-operand shared-memory stages of the encode MMA loop, 2 or 3
+ *   "encode_accbuf"   TMEM accumulator buffers of the encode kernel, 2 or 4 */
+int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value);
+int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* value);
 
 /* ---- whole products.
  * bcg_multiply: host buffers, synchronous; replaces fherma_run
