@@ -3,17 +3,10 @@
 // exception at the plugin boundary (native-smoke/solve.cu:46-49); here the C
 // ABI returns a code and the C++ plugin shim turns it back into an exception.
 #include "../../include/bytecrt_gb300.h"
-#include "engine.hpp"
+#include "capi_internal.hpp"
 
 #include <cstring>
 #include <new>
-
-struct bcg_plan {
-    bcg::HostPlan plan;
-};
-struct bcg_context {
-    std::unique_ptr<bcg::Context> ctx;
-};
 
 namespace {
 

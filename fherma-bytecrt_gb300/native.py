@@ -75,6 +75,7 @@ def lib():
         L.bcg_context_get_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.bcg_multiply.argtypes = [vp, _u32p, _u32p, _u32p, ctypes.c_uint32]
         L.bcg_multiply_device.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
+        L.bcg_multiply_device_static.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
         L.bcg_encode_device.argtypes = [vp, vp, vp, vp, vp, ctypes.c_size_t, ctypes.c_uint32, vp]
         L.bcg_negacyclic_device.argtypes = [vp, vp, vp, ctypes.c_size_t, ctypes.c_uint32, vp]
         L.bcg_crt_device.argtypes = [vp, vp, ctypes.c_size_t, vp, ctypes.c_uint32, vp]
@@ -201,6 +202,10 @@ class Multiplier:
     # ---- device buffers (torch tensors or raw addresses)
     def multiply_device(self, a, b, c, count: int, stream=None):
         _check(lib().bcg_multiply_device(self._h, _ptr(a), _ptr(b), _ptr(c), count, _ptr(stream)))
+
+    def multiply_device_static(self, a, b, c, count: int, stream=None):
+        """Like multiply_device, but allocates nothing (library-owned 16 MiB scratch)."""
+        _check(lib().bcg_multiply_device_static(self._h, _ptr(a), _ptr(b), _ptr(c), count, _ptr(stream)))
 
     def encode_device(self, a, b, planes_a, planes_b, plane_stride: int, count: int, stream=None):
         _check(lib().bcg_encode_device(self._h, _ptr(a), _ptr(b), _ptr(planes_a), _ptr(planes_b),

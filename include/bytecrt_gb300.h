@@ -85,6 +85,17 @@ int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_
 /* device buffers, asynchronous on `stream` */
 int bcg_multiply_device(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c,
                         uint32_t count, void* stream);
+/* Same product as bcg_multiply_device, for callers that cannot allocate
+ * device memory at call time (a caller-owned memory pool, a framework that
+ * forbids cudaMalloc on its hot path, an allocator already at its limit).
+ * No counterpart in the reference.  It allocates nothing: its residue-plane
+ * scratch is a 16 MiB array compiled into the library, held by every GPU that
+ * loads it.  A product needs 2*P*N words of it, so points up to N=32768 with
+ * W around 868 bits fit; larger points return BCG_ERR_INVALID.  The first call
+ * on a device looks up the array's device address (make it before any stream
+ * capture).  Calls that overlap on the GPU race on the shared array. */
+int bcg_multiply_device_static(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c,
+                               uint32_t count, void* stream);
 
 /* ---- pipeline stages (device buffers, asynchronous).  A residue plane set is
  * [P][N] uint32 per operand per product; sets of a batch are `plane_stride`
