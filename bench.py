@@ -8,11 +8,16 @@ seeded synthetic operands uniform in [0, q) standing in for the FHERMA
 challenge cases: 16 distinct products repeated to B, all larger than L2
 together (no L2 flush needed).
 
-  value : device-resident products/s (inputs already in HBM), K timed steps
-          bracketed by barrier + synchronize, CUDA events on the launching
-          stream, max over ranks.
-  e2e   : the same batch through the public host API (bcg_multiply) from
-          pinned host memory, H2D + compute + D2H inside the timed region.
+  value   : device-resident products/s (inputs already in HBM): each step is
+            one launch of the batch's CUDA graph (bcg_batch_run); K timed
+            steps bracketed by barrier + synchronize, CUDA events on the
+            launching stream, max over ranks.
+  e2e     : the same batch through the public host API (bcg_multiply) from
+            pinned host memory, H2D + compute + D2H inside the timed region.
+  plain   : one product per call (device-resident and host buffers).
+  uneven  : 96 products of two geometries and six moduli in one graph.
+  served  : the request loop (bcg_server_*) under seeded Poisson arrivals at
+            swept offered load: sustained products/s, p50/p99 latency.
 
 One JSON line on rank 0.  Under torchrun each rank runs its own batch on its
 own GPU (products shard with no collective: weak scaling).
@@ -212,13 +217,16 @@ def run_native(args):
     q, a_np, b_np = make_inputs(pkg, 1000 + 97 * rank)
     L = (W + 31) // 32
     m = pkg.Multiplier(N, W, q, device=local)
+    if args.group:
+        m.set_group(args.group)
+    group = m.get_tuning("group")
     info = m.info
 
     a_dev = tile_to(torch.from_numpy(a_np.view(np.int32)).cuda(), B)
     b_dev = tile_to(torch.from_numpy(b_np.view(np.int32)).cuda(), B)
     c_dev = torch.empty_like(a_dev)
     # A dedicated stream: the kernels and the timing events share it (a NULL
-    # stream handle would select the context's own stream instead).
+    # stream handle would select the library's own stream instead).
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
 
@@ -233,34 +241,42 @@ def run_native(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return float(t.item())
 
-    # ---- device-resident batched throughput.
-    for _ in range(args.warmup):
-        m.multiply_device(a_dev, b_dev, c_dev, B, stream=stream.cuda_stream)
-    torch.cuda.synchronize()
-    m.read_profile(reset=True)
-    m.profile(True)
-    barrier()
-    torch.cuda.synchronize()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        start.record(stream)
-        for _ in range(args.steps):
-            m.multiply_device(a_dev, b_dev, c_dev, B, stream=stream.cuda_stream)
-        end.record(stream)
+    def timed(fn, steps):
+        barrier()
         torch.cuda.synchronize()
-    barrier()
-    ms = max_over_ranks(start.elapsed_time(end))
-    prof = m.read_profile(reset=True)
-    m.profile(False)
-    m.synchronize()
-    value = world * B * args.steps / (ms / 1000.0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(steps):
+            fn()
+        e.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return max_over_ranks(s.elapsed_time(e))
 
-    # Spot-check one product of the timed batch against the first product's oracle? The
-    # parity suite covers exactness; here only a cheap self-consistency check of repeats.
+    # ---- batched B=128, one CUDA graph per step (the headline value).
+    batch = pkg.Batch(local)
+    batch.add(N, W, q, a_dev, b_dev, c_dev, B)
+    batch.profile(every=args.profile_every)
+    for _ in range(args.warmup):
+        batch.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        ms = timed(lambda: batch.run(stream.cuda_stream), args.steps)
+    prof = batch.read_profile()       # stage times of the last timed run
+    binfo = batch.info()
+    value = world * B * args.steps / (ms / 1000.0)
     c0 = c_dev[0].cpu()
     assert torch.equal(c0, c_dev[DISTINCT].cpu()), "repeated inputs gave different products"
 
-    # ---- plain single product (config: N=65536 plain path).
+    # ---- the same batch issued as stream launches (no graph), for comparison.
+    for _ in range(2):
+        m.multiply_device(a_dev, b_dev, c_dev, B, stream=stream.cuda_stream)
+    stream_ms = timed(lambda: m.multiply_device(a_dev, b_dev, c_dev, B, stream=stream.cuda_stream),
+                      max(3, args.steps // 2))
+    stream_value = world * B * max(3, args.steps // 2) / (stream_ms / 1000.0)
+    assert torch.equal(c_dev[0].cpu(), c0), "graph and stream launches disagree"
+
+    # ---- plain single product (the per-product baseline).
     plain_iters = max(3, args.steps)
     for _ in range(2):
         m.multiply_device(a_dev, b_dev, c_dev, 1, stream=stream.cuda_stream)
@@ -290,26 +306,29 @@ def run_native(args):
     barrier()
     e2e_value = world * B * args.steps / e2e_s
     assert torch.equal(c_h[0], c0), "host path and device path disagree"
-    # plain e2e (one product per call)
     for _ in range(2):
         m.multiply_into(a_h[0], b_h[0], c_h[0], 1)
     t0 = time.perf_counter()
     for i in range(plain_iters):
         m.multiply_into(a_h[i % DISTINCT], b_h[i % DISTINCT], c_h[i % DISTINCT], 1)
     plain_e2e_ms = 1000 * (time.perf_counter() - t0) / plain_iters
+    del a_h, b_h, c_h
+
+    uneven = run_uneven(pkg, args, stream, local) if args.uneven else None
+    served = run_served(pkg, args, local, value) if args.served else None
 
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
 
-    # ---- roofline of the dominant kernel, from the live per-stage events.
+    # ---- roofline of the dominant kernel, from the CUDA events inside the graph.
     alg = algorithmic(info)
-    stage_ms = prof["ms"]
+    per_launch = {s: prof["ms"][s] / prof["timed"][s] for s in prof["ms"] if prof["timed"][s]}
     launches = prof["launches"]
-    dominant = max(stage_ms, key=lambda s: stage_ms[s])
-    per_launch_ms = stage_ms[dominant] / max(1, launches[dominant])
-    products_per_launch = B * args.steps / max(1, launches[dominant])
+    dominant = max(per_launch, key=lambda s: per_launch[s] * launches[s])
+    per_launch_ms = per_launch[dominant]
+    products_per_launch = B / max(1, launches[dominant])
     alg_bytes = alg[dominant] * products_per_launch
     achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = load_peaks()
@@ -319,7 +338,9 @@ def run_native(args):
         "traffic": traffic * products_per_launch if traffic else None,
         "kernel": dominant, "peak_source": peak_kind,
         "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": per_launch_ms,
-        "stage_ms_per_product": {s: stage_ms[s] / (B * args.steps) for s in stage_ms},
+        "products_per_launch": products_per_launch,
+        "stage_ms_per_product": {s: per_launch[s] * launches[s] / B for s in per_launch},
+        "timed_launches": prof["timed"][dominant], "profile_every": args.profile_every,
     }
     cpu = cpu_baseline(pkg, q, a_np, b_np, sample=args.cpu_sample) if args.cpu_sample > 0 else None
     line = {
@@ -327,23 +348,176 @@ def run_native(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / PUBLISHED_BATCHED, "dtype": "u32",
         "data": "synthetic (seeded uniform operands in [0,q), seeded odd 1747-bit q; 16 distinct products repeated)",
-        "config": {"workload": "batched B=128 exact negacyclic products, N=65536 W=1747 L=55 P=114, one q",
-                   "global_batch": B * world, "per_gpu_batch": B, "group": info.group,
+        "config": {"workload": "batched B=128 exact negacyclic products, N=65536 W=1747 L=55 P=114, one q, "
+                               "one CUDA graph per step",
+                   "global_batch": B * world, "per_gpu_batch": B, "group": group,
                    "l2": "inputs larger than L2 (3.7 GB per step), no flush", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": 2 * B * N * L * 4,
                 "d2h_bytes_per_step": B * N * L * 4, "api": "bcg_multiply (host buffers, pinned)"},
+        "stream_launch": {"products_per_s": stream_value, "ms_per_step": stream_ms / max(3, args.steps // 2)},
         "plain": {"device_ms_per_product": plain_ms, "device_products_per_s": 1000.0 / plain_ms,
                   "e2e_ms_per_product": plain_e2e_ms, "e2e_products_per_s": 1000.0 / plain_e2e_ms,
                   "batched_over_plain_device": value / world / (1000.0 / plain_ms),
                   "batched_over_plain_e2e": e2e_value / world / (1000.0 / plain_e2e_ms)},
+        "uneven": uneven,
+        "served": served,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
-        "gpu_launches": sum(launches.values()),
+        "gpu_launches": binfo["launches"] * args.steps,
     }
     print(json.dumps(line), flush=True)
+    batch.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_uneven(pkg, args, stream, device):
+    """96 products in one graph: 58 at N=32768/W=868 and 38 at N=65536/W=1747,
+    three seeded moduli per geometry, four distinct operand pairs per modulus."""
+    import numpy as np
+    import torch
+    batch = pkg.Batch(device)
+    keep = []
+    total_bytes = 0
+    for (n, w), counts in (((32768, 868), (20, 19, 19)), ((65536, 1747), (13, 13, 12))):
+        for k, count in enumerate(counts):
+            q = pkg.inputs.modulus(w, 4000 + 10 * k + w)
+            a = np.stack([pkg.inputs.uniform(q, n, 7000 + 2 * i) for i in range(4)])
+            b = np.stack([pkg.inputs.uniform(q, n, 7001 + 2 * i) for i in range(4)])
+            ad = tile_to(torch.from_numpy(a.view(np.int32)).cuda(), count)
+            bd = tile_to(torch.from_numpy(b.view(np.int32)).cuda(), count)
+            cd = torch.empty_like(ad)
+            batch.add(n, w, q, ad, bd, cd, count)
+            keep.append((ad, bd, cd))
+            total_bytes += 3 * ad.numel() * 4
+    for _ in range(args.warmup):
+        batch.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(args.steps):
+        batch.run(stream.cuda_stream)
+    e.record(stream)
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / args.steps
+    info = batch.info()
+    batch.close()
+    return {"workload": "96 products: 58 at N=32768/W=868, 38 at N=65536/W=1747, 3 moduli per geometry, "
+                        "one CUDA graph per step, device-resident",
+            "products_per_s": 96 / (ms / 1000.0), "ms_per_step": ms, "groups": info["groups"],
+            "chains": info["chains"], "launches": info["launches"], "io_bytes": total_bytes}
+
+
+def run_served(pkg, args, device, batched_value):
+    """Served request loop: seeded Poisson arrivals at swept offered load, 30%
+    N=16384/W=434, 40% N=32768/W=868, 30% N=65536/W=1747 over 5 moduli; half
+    the requests reuse a resident left operand.  Latency is submission to
+    completion (host clock) including H2D, compute and D2H from pinned memory."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(77)
+    srv = pkg.Server(device, slots=3)
+    mix = [((16384, 434), 0.3, 1), ((32768, 868), 0.4, 2), ((65536, 1747), 0.3, 2)]
+    points = []   # (n, w, q, pid, a pool, b pool, resident ids, out ring)
+    for (n, w), share, nq in mix:
+        for k in range(nq):
+            q = pkg.inputs.modulus(w, 9000 + 17 * k + w)
+            pid = srv.add_point(n, w, q)
+            l = (w + 31) // 32
+            pool = torch.empty((8, n, l), dtype=torch.int32).pin_memory()
+            for i in range(8):
+                pool[i].copy_(torch.from_numpy(pkg.inputs.uniform(q, n, 100 * k + i).view(np.int32)))
+            res = [srv.add_operand(pid, pool[i]) for i in (0, 1)]
+            ring = torch.empty((48, n, l), dtype=torch.int32).pin_memory()
+            points.append(dict(n=n, w=w, q=q, pid=pid, pool=pool, res=res, ring=ring, share=share / nq,
+                               slot=0, owner=[None] * 48))
+    shares = np.array([p["share"] for p in points])
+    # Work per product relative to N=65536 (N * P, P ~ N * W): capacity estimate for the sweep.
+    rel = np.array([(p["n"] * (2 * p["w"] + 20)) / (65536 * 3514.0) for p in points])
+    capacity = batched_value / float((shares * rel).sum())
+    loads = [float(x) for x in args.served_loads.split(",")]
+    # Alone results for the combinations a request can draw (operand a from pool[0..1]
+    # resident or pool[2..3] sent, operand b from pool[4..7]), for verification.
+    alone = {}
+    for pi, p in enumerate(points):
+        mult = pkg.Multiplier(p["n"], p["w"], p["q"], device=device)
+        for ai in range(4):
+            for bi in range(4, 8):
+                alone[(pi, ai, bi)] = mult.multiply(p["pool"][ai].numpy().view(np.uint32),
+                                                   p["pool"][bi].numpy().view(np.uint32))
+        mult.close()
+    results = []
+    for frac in loads:
+        rate = frac * capacity
+        count = int(min(args.served_requests, max(200, rate * args.served_seconds)))
+        gaps = rng.exponential(1.0 / rate, size=count)
+        which = rng.choice(len(points), size=count, p=shares / shares.sum())
+        use_res = rng.random(count) < 0.5
+        pending = []   # (request id, point index, ai, bi, ring slot)
+        lat = []
+        verified = failed_checks = 0
+
+        def finish(entry):
+            nonlocal verified, failed_checks
+            rid, pi, ai, bi, slot = entry
+            lat.append(srv.wait(rid))
+            if verified < args.served_verify:
+                got = points[pi]["ring"][slot].numpy().view(np.uint32)
+                if not np.array_equal(got, alone[(pi, ai, bi)]):
+                    failed_checks += 1
+                verified += 1
+
+        srv_before = srv.stats()
+        t_start = time.perf_counter()
+        t_next = t_start
+        for i in range(count):
+            t_next += gaps[i]
+            while True:   # wait for the arrival time (sleep, then spin the last half millisecond)
+                left = t_next - time.perf_counter()
+                if left <= 0:
+                    break
+                if left > 0.0005:
+                    time.sleep(0.0002)
+            pi = int(which[i])
+            p = points[pi]
+            slot = p["slot"]
+            p["slot"] = (slot + 1) % len(p["owner"])
+            owner = p["owner"][slot]
+            if owner is not None:   # ring slot still in use: that request must finish first
+                idx = next(k for k, e in enumerate(pending) if e[0] == owner)
+                finish(pending.pop(idx))
+            bi = 4 + int(rng.integers(4))
+            if use_res[i]:
+                ai = int(rng.integers(2))
+                rid = srv.submit(p["pid"], p["pool"][bi], p["ring"][slot], operand=p["res"][ai])
+            else:
+                ai = 2 + int(rng.integers(2))
+                rid = srv.submit(p["pid"], p["pool"][bi], p["ring"][slot], a=p["pool"][ai])
+            p["owner"][slot] = rid
+            pending.append((rid, pi, ai, bi, slot))
+        for entry in pending:
+            finish(entry)
+        elapsed = time.perf_counter() - t_start
+        for p in points:
+            p["owner"] = [None] * len(p["owner"])
+        st = srv.stats()
+        batches = st["batches"] - srv_before["batches"]
+        lat_ms = np.array(lat)
+        results.append({"offered_fraction": frac, "offered_per_s": rate, "requests": count,
+                        "sustained_per_s": count / elapsed,
+                        "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+                        "mean_batch": count / max(1, batches), "verified": verified,
+                        "mismatches": failed_checks})
+    stats = srv.stats()
+    srv.close()
+    best = max(results, key=lambda r: r["sustained_per_s"])
+    return {"workload": "Poisson arrivals; 30% N=16384/W=434, 40% N=32768/W=868, 30% N=65536/W=1747; "
+                        "5 moduli (1/2/2); 50% reuse a resident left operand; host buffers (pinned)",
+            "capacity_estimate_per_s": capacity, "sweep": results,
+            "sustained_per_s": best["sustained_per_s"], "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"],
+            "memory_budget": stats["memory_budget"], "memory_peak": stats["memory_peak"],
+            "rejected": stats["rejected"], "failed": stats["failed"]}
 
 
 def run_profile_case(args):
@@ -377,6 +551,17 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4, help="products in the CPU baseline sample (0: skip)")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu case and exit")
     ap.add_argument("--profile-count", type=int, default=2)
+    ap.add_argument("--group", type=int, default=0, help="products per launch chain (0: library default)")
+    ap.add_argument("--profile-every", type=int, default=2,
+                    help="time the stages of every k-th launch chain with CUDA events")
+    ap.add_argument("--no-uneven", dest="uneven", action="store_false", help="skip the uneven 96-product batch")
+    ap.add_argument("--no-served", dest="served", action="store_false", help="skip the served sweep")
+    ap.add_argument("--served-loads", default="0.25,0.5,0.75,0.9",
+                    help="offered loads as fractions of the estimated capacity")
+    ap.add_argument("--served-seconds", type=float, default=1.5, help="arrival window per offered load")
+    ap.add_argument("--served-requests", type=int, default=20000, help="cap on requests per offered load")
+    ap.add_argument("--served-verify", type=int, default=64,
+                    help="responses per load compared with the same product run alone")
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)

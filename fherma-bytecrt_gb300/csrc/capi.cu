@@ -8,30 +8,10 @@
 #include <cstring>
 #include <new>
 
-namespace {
+using bcg::guarded;
+using bcg::require;
 
-template <class F>
-int guarded(F&& f) {
-    try {
-        f();
-        return BCG_OK;
-    } catch (const std::invalid_argument& e) {
-        bcg::set_last_error(e.what());
-        return BCG_ERR_INVALID;
-    } catch (const bcg::DeviceTimeout& e) {
-        bcg::set_last_error(e.what());
-        return BCG_ERR_DEVICE_TIMEOUT;
-    } catch (const bcg::CudaError& e) {
-        bcg::set_last_error(e.what());
-        return (e.code == cudaErrorMemoryAllocation) ? BCG_ERR_NOMEM : BCG_ERR_CUDA;
-    } catch (const std::bad_alloc& e) {
-        bcg::set_last_error("host allocation failed");
-        return BCG_ERR_NOMEM;
-    } catch (const std::exception& e) {
-        bcg::set_last_error(e.what());
-        return BCG_ERR_INVALID;
-    }
-}
+namespace {
 
 void fill_info(const bcg::HostPlan& p, bcg_info* out, uint32_t group) {
     const bcg::Geometry& g = p.g;
@@ -43,9 +23,6 @@ void fill_info(const bcg::HostPlan& p, bcg_info* out, uint32_t group) {
     out->workspace_bytes_per_product = uint64_t(2) * g.P * g.N * 4;
 }
 
-void require(bool ok, const char* what) {
-    if (!ok) throw std::invalid_argument(what);
-}
 
 }  // namespace
 
@@ -203,7 +180,8 @@ int bcg_synchronize(bcg_context* ctx) {
 int bcg_profile_enable(bcg_context* ctx, int enable) {
     return guarded([&] {
         require(ctx, "null context");
-        ctx->ctx->set_profiling(enable != 0);
+        require(enable >= 0, "profile sampling period must be >= 0");
+        ctx->ctx->set_profiling(uint32_t(enable));
     });
 }
 
@@ -211,7 +189,7 @@ int bcg_profile_read(bcg_context* ctx, bcg_profile* out, int reset) {
     return guarded([&] {
         require(ctx && out, "null argument");
         std::memset(out, 0, sizeof *out);
-        ctx->ctx->read_profile(out->ms, out->launches, &out->chains, reset != 0);
+        ctx->ctx->read_profile(out->ms, out->launches, out->timed, &out->chains, reset != 0);
     });
 }
 

@@ -3,6 +3,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <omp.h>
 
 namespace bcg {
@@ -26,6 +29,26 @@ void parallel_copy(void* dst, const void* src, size_t bytes) {
 }
 }  // namespace
 
+std::shared_ptr<const GeometryTables> geometry_tables(int device, const HostPlan& plan) {
+    // Weak entries: the tables live as long as some Context of the geometry does.
+    static std::mutex mu;
+    static std::map<std::tuple<int, uint32_t, uint32_t, uint32_t>, std::weak_ptr<const GeometryTables>> cache;
+    const auto key = std::make_tuple(device, plan.g.N, plan.g.W, plan.g.L);
+    std::lock_guard<std::mutex> lock(mu);
+    if (auto hit = cache[key].lock()) return hit;
+    auto t = std::make_shared<GeometryTables>();
+    auto upload = [&](DeviceBuffer& buf, const void* src, size_t bytes) {
+        buf.allocate(bytes);
+        check(cudaMemcpy(buf.ptr, src, bytes, cudaMemcpyHostToDevice), "table upload");
+    };
+    upload(t->consts, plan.prime_consts.data(), plan.prime_consts.size() * 4);
+    upload(t->tables, plan.ntt_tables.data(), plan.ntt_tables.size() * 4);
+    upload(t->enc_b, plan.enc_b.data(), plan.enc_b.size() * 2);
+    upload(t->invp, plan.invp.data(), plan.invp.size() * 4);
+    cache[key] = t;
+    return t;
+}
+
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 const char* last_error() { return g_last_error.c_str(); }
 
@@ -45,18 +68,15 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
         buf.allocate(bytes);
         check(cudaMemcpy(buf.ptr, src, bytes, cudaMemcpyHostToDevice), "table upload");
     };
-    upload(consts_, plan_.prime_consts.data(), plan_.prime_consts.size() * 4);
-    upload(tables_, plan_.ntt_tables.data(), plan_.ntt_tables.size() * 4);
-    upload(enc_b_, plan_.enc_b.data(), plan_.enc_b.size() * 2);
+    geo_ = geometry_tables(device_, plan_);
     upload(crt_b_, plan_.crt_b.data(), plan_.crt_b.size() * 2);
-    upload(invp_, plan_.invp.data(), plan_.invp.size() * 4);
     upload(q_, plan_.q.data(), plan_.q.size() * 4);
     status_.allocate(16);
     check(cudaMemset(status_.ptr, 0, 16), "status reset");
 
     const TableOffsets off = table_offsets(g);
-    ntt_.consts = consts_.as<uint4>();
-    ntt_.tables = tables_.as<uint2>();
+    ntt_.consts = geo_->consts.as<uint4>();
+    ntt_.tables = geo_->tables.as<uint2>();
     ntt_.table_stride = g.table_stride;
     ntt_.off_col_f = off.col_f; ntt_.off_col_i = off.col_i;
     ntt_.off_row_f = off.row_f; ntt_.off_row_i = off.row_i;
@@ -64,21 +84,23 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     ntt_.off_itw_lo = off.itw_lo; ntt_.off_itw_hi = off.itw_hi;
     ntt_.N = g.N; ntt_.P = g.P; ntt_.c_bits = g.c_bits; ntt_.z_bits = g.z_bits; ntt_.Z = g.Z; ntt_.H = g.H;
 
-    enc_.enc_b = enc_b_.as<uint16_t>();
+    enc_.enc_b = geo_->enc_b.as<uint16_t>();
     for (uint32_t j = 0; j < g.P; ++j)
         enc_.prime[j] = make_uint2(plan_.prime_consts[4 * j], plan_.prime_consts[4 * j + 1]);
     enc_.N = g.N; enc_.L = g.L; enc_.P = g.P; enc_.K = g.enc_k; enc_.cols = g.enc_cols; enc_.chunks = g.enc_chunks;
     enc_.status = status_.as<uint32_t>();
 
     crt_.crt_b = crt_b_.as<uint16_t>();
-    crt_.invp = invp_.as<float>();
+    crt_.invp = geo_->invp.as<float>();
     for (uint32_t l = 0; l < g.L; ++l) crt_.q[l] = plan_.q[l];
     crt_.q_inv_scaled = plan_.q_inv_scaled;
     crt_.N = g.N; crt_.L = g.L; crt_.P = g.P; crt_.k_total = g.crt_k_total; crt_.kchunks = g.crt_kchunks;
     crt_.E = g.crt_e; crt_.NC = g.crt_n;
     crt_.status = status_.as<uint32_t>();
 
-    group_ = std::max<uint32_t>(1, 65536 / g.N);
+    // Products per launch chain: long chains amortise each kernel's launch and
+    // tail (8 products per chain at N=65536 measured 16% faster than 1).
+    group_ = std::min<uint32_t>(256, std::max<uint32_t>(1, 524288 / g.N));
 }
 
 Context::~Context() {
@@ -180,7 +202,8 @@ void Context::crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint3
 void Context::mark_begin(int stage, cudaStream_t st) {
     ++stage_launches_[stage];
     ++launches_total_;
-    if (!profiling_) return;
+    if (!timing_chain_) return;
+    ++stage_timed_[stage];
     auto take = [&]() {
         if (event_pool_.empty()) {
             cudaEvent_t e;
@@ -197,11 +220,11 @@ void Context::mark_begin(int stage, cudaStream_t st) {
 }
 
 void Context::mark_end(cudaStream_t st) {
-    if (!profiling_ || marks_.empty()) return;
+    if (!timing_chain_ || marks_.empty()) return;
     check(cudaEventRecord(marks_.back().end, st), "profile event");
 }
 
-void Context::read_profile(double* ms, uint64_t* launches, uint64_t* chains, bool reset) {
+void Context::read_profile(double* ms, uint64_t* launches, uint64_t* timed, uint64_t* chains, bool reset) {
     for (int s = 0; s < kStages; ++s) ms[s] = 0;
     for (const Mark& m : marks_) {
         check(cudaEventSynchronize(m.end), "profile event");
@@ -209,44 +232,54 @@ void Context::read_profile(double* ms, uint64_t* launches, uint64_t* chains, boo
         check(cudaEventElapsedTime(&t, m.begin, m.end), "profile elapsed");
         ms[m.stage] += t;
     }
-    for (int s = 0; s < kStages; ++s) launches[s] = stage_launches_[s];
+    for (int s = 0; s < kStages; ++s) { launches[s] = stage_launches_[s]; timed[s] = stage_timed_[s]; }
     *chains = chains_;
     if (reset) {
         for (const Mark& m : marks_) { event_pool_.push_back(m.begin); event_pool_.push_back(m.end); }
         marks_.clear();
         for (auto& l : stage_launches_) l = 0;
+        for (auto& l : stage_timed_) l = 0;
         chains_ = 0;
     }
 }
 
 void Context::chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, uint32_t* ws,
-                    cudaStream_t st) {
+                    cudaStream_t st, StageTimer* timer) {
     // Workspace per product: [A planes | B planes]; the product overwrites A.
     const size_t pw = plane_words();
     uint32_t* pa = ws;
     uint32_t* pb = ws + pw;
     const size_t stride = 2 * pw;
     ++chains_;
-    mark_begin(kEncode, st);
+    timing_chain_ = timer == nullptr && profile_every_ != 0 && (chains_ - 1) % profile_every_ == 0;
+    auto begin = [&](int stage) {
+        if (timer) { ++stage_launches_[stage]; ++launches_total_; timer->begin(stage, st); }
+        else mark_begin(stage, st);
+    };
+    auto end = [&] {
+        if (timer) timer->end(st);
+        else mark_end(st);
+    };
+    begin(kEncode);
     encode(a, b, pa, pb, stride, count, st);
-    mark_end(st);
+    end();
     // Both operands' column passes in one launch (sets alternate A, B).
     if (geom().C > 1) {
-        mark_begin(kColForward, st);
+        begin(kColForward);
         check(launch_col_forward(ntt_, pa, pw, 2 * count, st), "column pass launch");
-        mark_end(st);
+        end();
     }
-    mark_begin(kRow, st);
+    begin(kRow);
     check(launch_row_product(ntt_, pa, stride, pb, stride, pa, stride, count, false, st), "row pass launch");
-    mark_end(st);
+    end();
     if (geom().C > 1) {
-        mark_begin(kColInverse, st);
+        begin(kColInverse);
         check(launch_col_inverse(ntt_, pa, stride, count, st), "inverse column pass launch");
-        mark_end(st);
+        end();
     }
-    mark_begin(kCrt, st);
+    begin(kCrt);
     crt(pa, stride, c, count, st);
-    mark_end(st);
+    end();
 }
 
 void Context::forward_spectral(const uint32_t* x, uint32_t* planes, cudaStream_t st) {

@@ -30,6 +30,13 @@ public:
     using std::runtime_error::runtime_error;
 };
 
+// Admission refused by the serving loop (queue full, or a request larger
+// than the memory budget).
+class Busy : public std::runtime_error {
+public:
+    using std::runtime_error::runtime_error;
+};
+
 inline void check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw CudaError(what, e);
 }
@@ -40,6 +47,7 @@ struct DeviceBuffer {
     DeviceBuffer() = default;
     DeviceBuffer(const DeviceBuffer&) = delete;
     DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr(o.ptr), bytes(o.bytes) { o.ptr = nullptr; o.bytes = 0; }
     ~DeviceBuffer() { if (ptr) cudaFree(ptr); }
     void allocate(size_t n) {
         if (ptr) { cudaFree(ptr); ptr = nullptr; bytes = 0; }
@@ -60,6 +68,23 @@ struct PinnedBuffer {
         if (n) { check(cudaMallocHost(&ptr, n), "pinned allocation"); bytes = n; }
     }
     template <class T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Device tables that depend only on the geometry (N, W, L) and the device:
+// prime constants, NTT twiddle/twist tables, the encode B operand and 1/p_j.
+// Every Context of the same geometry on a device shares one copy (moduli of a
+// geometry differ only in the CRT weights and q, which stay per Context).
+struct GeometryTables {
+    DeviceBuffer consts, tables, enc_b, invp;
+};
+std::shared_ptr<const GeometryTables> geometry_tables(int device, const HostPlan& plan);
+
+// Receives the stage boundaries of a launch chain (per-stage CUDA-event timing).
+class StageTimer {
+public:
+    virtual ~StageTimer() = default;
+    virtual void begin(int stage, cudaStream_t st) = 0;
+    virtual void end(cudaStream_t st) = 0;
 };
 
 class Context {
@@ -99,7 +124,9 @@ public:
     void check_status();
 
     // One product chain on a caller-provided workspace of >= count products.
-    void chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, uint32_t* ws, cudaStream_t st);
+    // `timer` (optional) replaces the context's own sampled profiler for this chain.
+    void chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, uint32_t* ws, cudaStream_t st,
+               StageTimer* timer = nullptr);
 
     NttArgs ntt_args() const { return ntt_; }
     EncodeTuning& encode_tuning() { return enc_tuning_; }
@@ -107,19 +134,22 @@ public:
 
     // Per-stage timing with CUDA events recorded on the launching stream.
     enum Stage { kEncode = 0, kColForward, kRow, kColInverse, kCrt, kStages };
-    void set_profiling(bool on) { profiling_ = on; }
+    // every: 0 off, k > 0 brackets the stages of every k-th launch chain with events.
+    void set_profiling(uint32_t every) { profile_every_ = every; }
     // Sums the elapsed time of every recorded stage (synchronizes on them).
-    void read_profile(double* ms, uint64_t* launches, uint64_t* chains, bool reset);
+    void read_profile(double* ms, uint64_t* launches, uint64_t* timed, uint64_t* chains, bool reset);
     uint64_t launches() const { return launches_total_; }
 
 private:
     struct Mark { int stage; cudaEvent_t begin, end; };
     void mark_begin(int stage, cudaStream_t st);
     void mark_end(cudaStream_t st);
-    bool profiling_ = false;
+    uint32_t profile_every_ = 0;
+    bool timing_chain_ = false;
     std::vector<Mark> marks_;
     std::vector<cudaEvent_t> event_pool_;
     uint64_t stage_launches_[kStages] = {};
+    uint64_t stage_timed_[kStages] = {};
     uint64_t launches_total_ = 0, chains_ = 0;
 
     void ensure_workspace(uint32_t products);
@@ -132,7 +162,8 @@ private:
     cudaStream_t stream_ = nullptr;
     cudaStream_t copy_in_ = nullptr, copy_out_ = nullptr;
     uint32_t group_ = 1;
-    DeviceBuffer consts_, tables_, enc_b_, crt_b_, invp_, q_, status_;
+    std::shared_ptr<const GeometryTables> geo_;
+    DeviceBuffer crt_b_, q_, status_;
     DeviceBuffer ws_;
     size_t ws_products_ = 0;
     // Host-buffer path: double-buffered device inputs/outputs and pinned staging.

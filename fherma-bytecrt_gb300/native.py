@@ -21,6 +21,7 @@ BCG_ERR_CUDA = 2
 BCG_ERR_NOMEM = 3
 BCG_ERR_DEVICE_TIMEOUT = 4
 BCG_ERR_BUSY = 5
+BCG_ERR_TIMEOUT = 6
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 
@@ -38,7 +39,24 @@ class bcg_info(ctypes.Structure):
 
 
 class bcg_profile(ctypes.Structure):
-    _fields_ = [("ms", ctypes.c_double * 8), ("launches", ctypes.c_uint64 * 8), ("chains", ctypes.c_uint64)]
+    _fields_ = [("ms", ctypes.c_double * 8), ("launches", ctypes.c_uint64 * 8), ("timed", ctypes.c_uint64 * 8),
+                ("chains", ctypes.c_uint64)]
+
+
+class bcg_batch_info(ctypes.Structure):
+    _fields_ = [("groups", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("products", ctypes.c_uint64),
+                ("chains", ctypes.c_uint64), ("launches", ctypes.c_uint64)]
+
+
+class bcg_server_options(ctypes.Structure):
+    _fields_ = [("memory_bytes", ctypes.c_uint64), ("slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
+                ("max_queue", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class bcg_server_stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in
+                ("submitted", "completed", "failed", "rejected", "batches", "batched_products", "operands",
+                 "memory_budget", "memory_used", "memory_peak")]
 
 
 STAGES = ("encode", "column", "row", "column_inverse", "crt")
@@ -82,6 +100,26 @@ def lib():
         L.bcg_synchronize.argtypes = [vp]
         L.bcg_profile_enable.argtypes = [vp, ctypes.c_int]
         L.bcg_profile_read.argtypes = [vp, ctypes.POINTER(bcg_profile), ctypes.c_int]
+        u32, u64 = ctypes.c_uint32, ctypes.c_uint64
+        L.bcg_batch_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+        L.bcg_batch_destroy.argtypes = [vp]
+        L.bcg_batch_destroy.restype = None
+        L.bcg_batch_add.argtypes = [vp, u32, u32, u32, _u32p, vp, vp, vp, u32]
+        L.bcg_batch_run.argtypes = [vp, vp]
+        L.bcg_batch_synchronize.argtypes = [vp, vp]
+        L.bcg_batch_get_info.argtypes = [vp, ctypes.POINTER(bcg_batch_info)]
+        L.bcg_batch_profile_enable.argtypes = [vp, ctypes.c_int]
+        L.bcg_batch_profile_read.argtypes = [vp, ctypes.POINTER(bcg_profile)]
+        L.bcg_server_create.argtypes = [ctypes.c_int, ctypes.POINTER(bcg_server_options), ctypes.POINTER(vp)]
+        L.bcg_server_destroy.argtypes = [vp]
+        L.bcg_server_destroy.restype = None
+        L.bcg_server_add_point.argtypes = [vp, u32, u32, u32, _u32p, ctypes.POINTER(u32)]
+        L.bcg_server_add_operand.argtypes = [vp, u32, vp, ctypes.POINTER(u64)]
+        L.bcg_server_remove_operand.argtypes = [vp, u64]
+        L.bcg_server_submit.argtypes = [vp, u32, vp, u64, vp, vp, ctypes.POINTER(u64)]
+        L.bcg_server_wait.argtypes = [vp, u64, u32, ctypes.POINTER(ctypes.c_double)]
+        L.bcg_server_drain.argtypes = [vp]
+        L.bcg_server_get_stats.argtypes = [vp, ctypes.POINTER(bcg_server_stats)]
         _lib = L
     return _lib
 
@@ -222,12 +260,123 @@ class Multiplier:
         _check(lib().bcg_synchronize(self._h))
 
     # ---- measurement
-    def profile(self, enable: bool = True):
-        _check(lib().bcg_profile_enable(self._h, 1 if enable else 0))
+    def profile(self, enable: bool = True, every: int = 1):
+        """Time the stages of every `every`-th launch chain with CUDA events (off: enable=False)."""
+        _check(lib().bcg_profile_enable(self._h, int(every) if enable else 0))
 
     def read_profile(self, reset: bool = True) -> dict:
         p = bcg_profile()
         _check(lib().bcg_profile_read(self._h, ctypes.byref(p), 1 if reset else 0))
-        return {"ms": {s: p.ms[i] for i, s in enumerate(STAGES)},
-                "launches": {s: int(p.launches[i]) for i, s in enumerate(STAGES)},
-                "chains": int(p.chains)}
+        return _profile_dict(p)
+
+
+def _hptr(x) -> int:
+    """Host address of a numpy array or a (pinned) CPU torch tensor."""
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        assert x.flags.c_contiguous
+        return x.ctypes.data
+    return x.data_ptr()
+
+
+def _profile_dict(p: "bcg_profile") -> dict:
+    return {"ms": {s: p.ms[i] for i, s in enumerate(STAGES)},
+            "launches": {s: int(p.launches[i]) for i, s in enumerate(STAGES)},
+            "timed": {s: int(p.timed[i]) for i, s in enumerate(STAGES)},
+            "chains": int(p.chains)}
+
+
+class Batch:
+    """Products of uneven points in one CUDA graph (bcg_batch_*)."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib().bcg_batch_create(int(device), ctypes.byref(h)))
+        self._h = h
+        self._keep = []   # moduli and buffers referenced by the graph
+
+    def add(self, N: int, W: int, q, a, b, c, count: int):
+        q = np.ascontiguousarray(q, dtype=np.uint32)
+        self._keep.append((q, a, b, c))
+        _check(lib().bcg_batch_add(self._h, N, W, limbs(W), _p(q), _ptr(a), _ptr(b), _ptr(c), count))
+
+    def run(self, stream=None):
+        _check(lib().bcg_batch_run(self._h, _ptr(stream)))
+
+    def synchronize(self, stream=None):
+        _check(lib().bcg_batch_synchronize(self._h, _ptr(stream)))
+
+    def info(self) -> dict:
+        i = bcg_batch_info()
+        _check(lib().bcg_batch_get_info(self._h, ctypes.byref(i)))
+        return {"groups": i.groups, "products": i.products, "chains": i.chains, "launches": i.launches}
+
+    def profile(self, every: int = 1):
+        _check(lib().bcg_batch_profile_enable(self._h, int(every)))
+
+    def read_profile(self) -> dict:
+        p = bcg_profile()
+        _check(lib().bcg_batch_profile_read(self._h, ctypes.byref(p)))
+        return _profile_dict(p)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bcg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Server:
+    """Request loop with continuous batching on one GPU (bcg_server_*)."""
+
+    def __init__(self, device: int = 0, memory_bytes: int = 0, slots: int = 0, max_batch: int = 0,
+                 max_queue: int = 0):
+        o = bcg_server_options(memory_bytes, slots, max_batch, max_queue, 0)
+        h = ctypes.c_void_p()
+        _check(lib().bcg_server_create(int(device), ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+
+    def add_point(self, N: int, W: int, q) -> int:
+        q = np.ascontiguousarray(q, dtype=np.uint32)
+        out = ctypes.c_uint32()
+        _check(lib().bcg_server_add_point(self._h, N, W, limbs(W), _p(q), ctypes.byref(out)))
+        return out.value
+
+    def add_operand(self, point: int, a) -> int:
+        out = ctypes.c_uint64()
+        _check(lib().bcg_server_add_operand(self._h, point, _hptr(a), ctypes.byref(out)))
+        return out.value
+
+    def remove_operand(self, operand: int):
+        _check(lib().bcg_server_remove_operand(self._h, operand))
+
+    def submit(self, point: int, b, c, a=None, operand: int = 0) -> int:
+        out = ctypes.c_uint64()
+        _check(lib().bcg_server_submit(self._h, point, None if a is None else _hptr(a), operand, _hptr(b),
+                                       _hptr(c), ctypes.byref(out)))
+        return out.value
+
+    def wait(self, request: int, timeout_ms: int = 0) -> float:
+        """Latency in ms; raises BcgError with the request's own status on failure."""
+        lat = ctypes.c_double()
+        _check(lib().bcg_server_wait(self._h, request, timeout_ms, ctypes.byref(lat)))
+        return lat.value
+
+    def drain(self):
+        _check(lib().bcg_server_drain(self._h))
+
+    def stats(self) -> dict:
+        s = bcg_server_stats()
+        _check(lib().bcg_server_get_stats(self._h, ctypes.byref(s)))
+        return {n: int(getattr(s, n)) for n, _ in bcg_server_stats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bcg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -35,6 +35,7 @@ extern "C" {
 #define BCG_ERR_NOMEM 3          /* device or pinned allocation failed */
 #define BCG_ERR_DEVICE_TIMEOUT 4 /* a kernel's bounded wait ran out (context stays usable) */
 #define BCG_ERR_BUSY 5           /* admission refused (server) */
+#define BCG_ERR_TIMEOUT 6        /* bcg_server_wait: the request has not completed yet */
 
 typedef struct bcg_plan bcg_plan;        /* host-only plan (no GPU needed) */
 typedef struct bcg_context bcg_context;  /* plan + device tables + workspace */
@@ -120,17 +121,90 @@ int bcg_crt_device(bcg_context* ctx, const uint32_t* terms, size_t plane_stride,
 int bcg_synchronize(bcg_context* ctx);
 
 /* ---- measurement.  Stage order: 0 encode, 1 column pass, 2 row pass,
- * 3 inverse column pass, 4 CRT.  With profiling on, every stage launch is
- * bracketed by CUDA events on its own stream (the reference times its phases
- * the same way on warm-up calls, native-smoke/solve.cu:406-503). */
+ * 3 inverse column pass, 4 CRT.  bcg_profile_enable(ctx, k): k = 0 turns
+ * profiling off; k > 0 brackets every stage launch of every k-th launch chain
+ * with CUDA events on its own stream (the reference times its phases the same
+ * way on warm-up calls, native-smoke/solve.cu:406-503).  A period above 1
+ * keeps the event records from stretching the region being timed. */
 #define BCG_STAGES 5
 typedef struct bcg_profile {
-    double ms[8];           /* summed device time per stage */
+    double ms[8];           /* summed device time of the timed launches, per stage */
     uint64_t launches[8];   /* kernel launches per stage */
+    uint64_t timed[8];      /* launches per stage that carried events */
     uint64_t chains;        /* launch chains issued */
 } bcg_profile;
-int bcg_profile_enable(bcg_context* ctx, int enable);
+int bcg_profile_enable(bcg_context* ctx, int every);
 int bcg_profile_read(bcg_context* ctx, bcg_profile* out, int reset);
+
+/* ---- batched form.  The reference's batched plugin runs B products of one
+ * point per fherma_run over four pipelined slots (native-batched/solve.cu:
+ * 17-34, :200-244).  A bcg_batch takes products of any points (device
+ * buffers), groups them by (geometry, q), and captures the launch chains of
+ * every group into one CUDA graph on the first run; every run is then one
+ * graph launch.  Contexts of one geometry share the twiddle, twist and encode
+ * tables; contexts of one q share the CRT weights.  Runs of one batch must
+ * not overlap (they share one workspace). */
+typedef struct bcg_batch bcg_batch;
+typedef struct bcg_batch_info {
+    uint32_t groups;        /* distinct (geometry, q) groups */
+    uint32_t reserved;
+    uint64_t products;
+    uint64_t chains;        /* launch chains per run */
+    uint64_t launches;      /* kernel launches per run */
+} bcg_batch_info;
+int bcg_batch_create(int device, bcg_batch** out);
+void bcg_batch_destroy(bcg_batch* batch);
+/* `count` products of one point: a, b, c device buffers [count][N][L], 16-byte
+ * aligned, kept valid while the batch runs.  Invalidates the captured graph. */
+int bcg_batch_add(bcg_batch* batch, uint32_t N, uint32_t W, uint32_t L, const uint32_t* q,
+                  const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
+int bcg_batch_run(bcg_batch* batch, void* stream);
+int bcg_batch_synchronize(bcg_batch* batch, void* stream);
+int bcg_batch_get_info(bcg_batch* batch, bcg_batch_info* out);   /* captures the graph if needed */
+/* Stage events inside the graph for every k-th chain (recaptures); the
+ * profile holds the stage times of the last completed run. */
+int bcg_batch_profile_enable(bcg_batch* batch, int every);
+int bcg_batch_profile_read(bcg_batch* batch, bcg_profile* out);
+
+/* ---- served form (no counterpart in the reference, which has no server).
+ * A request loop on one GPU with continuous batching: submitted products of
+ * any registered point wait in arrival order; whenever a slot stream is free
+ * the oldest request leads a batch with the later requests of the same point
+ * and resident operand, admitted only if its device bytes fit the free part
+ * of the memory budget; batches on different slots overlap.  Resident
+ * operands keep their forward-transformed residues on the device, so a
+ * request that names one skips its encode and forward transform.  Host
+ * buffers stay caller-owned and valid until the request is waited for. */
+typedef struct bcg_server bcg_server;
+typedef struct bcg_server_options {
+    uint64_t memory_bytes;  /* device memory budget; 0: 80% of the free memory */
+    uint32_t slots;         /* batches in flight (1..16); 0: 3 */
+    uint32_t max_batch;     /* products per batch; 0: the point's group */
+    uint32_t max_queue;     /* waiting requests before submit returns BCG_ERR_BUSY; 0: 65536 */
+    uint32_t reserved;
+} bcg_server_options;
+typedef struct bcg_server_stats {
+    uint64_t submitted, completed, failed, rejected;
+    uint64_t batches, batched_products, operands;
+    uint64_t memory_budget, memory_used, memory_peak;
+} bcg_server_stats;
+int bcg_server_create(int device, const bcg_server_options* opt, bcg_server** out);
+/* Finishes every submitted request, then stops. */
+void bcg_server_destroy(bcg_server* server);
+int bcg_server_add_point(bcg_server* server, uint32_t N, uint32_t W, uint32_t L, const uint32_t* q,
+                         uint32_t* point);
+/* Encodes and forward-transforms host operand a ([N][L]) once, synchronously. */
+int bcg_server_add_operand(bcg_server* server, uint32_t point, const uint32_t* a, uint64_t* operand);
+int bcg_server_remove_operand(bcg_server* server, uint64_t operand);
+/* c = a*b; pass a = NULL and operand != 0 to use a resident operand. */
+int bcg_server_submit(bcg_server* server, uint32_t point, const uint32_t* a, uint64_t operand,
+                      const uint32_t* b, uint32_t* c, uint64_t* request);
+/* Returns the request's own status (BCG_OK or its error), or BCG_ERR_TIMEOUT
+ * after timeout_ms (0: no limit) with the request still pending.  latency_ms:
+ * submission to completion on the host clock. */
+int bcg_server_wait(bcg_server* server, uint64_t request, uint32_t timeout_ms, double* latency_ms);
+int bcg_server_drain(bcg_server* server);
+int bcg_server_get_stats(const bcg_server* server, bcg_server_stats* out);
 
 #ifdef __cplusplus
 }

@@ -84,6 +84,26 @@ def test_context_without_gpu_fails_loudly():
     assert e.value.code in (pkg.BCG_ERR_CUDA, pkg.BCG_ERR_NOMEM)
 
 
+@pytest.mark.skipif(gpu_available(), reason="checks the no-GPU error path")
+def test_batch_and_server_without_gpu_fail_loudly():
+    pkg = package()
+    with pytest.raises(pkg.BcgError) as e:
+        pkg.Batch(0)
+    assert e.value.code == pkg.BCG_ERR_CUDA
+    with pytest.raises(pkg.BcgError) as e:
+        pkg.Server(0)
+    assert e.value.code == pkg.BCG_ERR_CUDA
+
+
+def test_batch_and_server_reject_null_handles():
+    L = package().lib()
+    assert L.bcg_batch_run(None, None) == 1
+    assert L.bcg_batch_add(None, 16, 64, 2, None, None, None, None, 1) == 1
+    assert L.bcg_server_submit(None, 1, None, 0, None, None, None) == 1
+    assert L.bcg_server_wait(None, 1, 0, None) == 1
+    assert L.bcg_server_drain(None) == 1
+
+
 def test_plugin_rejects_bad_points_before_touching_the_gpu():
     pkg = package()
     q = pkg.inputs.modulus(434, 1)
