@@ -138,9 +138,17 @@ int main(int argc, char** argv) {
             write_results(out_root, init_s, rows);
             continue;
         }
-        fs::create_directories(out_root / case_name(i));
-        std::ofstream f(out_root / case_name(i) / "c.bin", std::ios::binary);
-        f.write(reinterpret_cast<const char*>(answer.c.data.data()), std::streamsize(answer.c.data.size() * 4));
+        try {
+            fs::create_directories(out_root / case_name(i));
+            std::ofstream f(out_root / case_name(i) / "c.bin", std::ios::binary);
+            f.write(reinterpret_cast<const char*>(answer.c.data.data()), std::streamsize(answer.c.data.size() * 4));
+            if (!f) throw std::runtime_error("short write of c.bin");
+        } catch (const std::exception& e) {
+            rows.push_back("{\"i\":" + std::to_string(i) + ",\"seconds\":null,\"status\":\"crashed\",\"note\":\"" +
+                           json_escape(std::string("writing the answer: ") + e.what()) + "\"}");
+            write_results(out_root, init_s, rows);
+            continue;
+        }
         std::snprintf(row, sizeof row, "{\"i\":%zu,\"seconds\":%.9f,\"status\":\"ok\"}", i, seconds);
         rows.push_back(row);
         write_results(out_root, init_s, rows);
