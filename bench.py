@@ -217,6 +217,9 @@ def run_native(args):
     q, a_np, b_np = make_inputs(pkg, 1000 + 97 * rank)
     L = (W + 31) // 32
     m = pkg.Multiplier(N, W, q, device=local)
+    # The autotuner picks this geometry's kernel shapes; the batch's contexts
+    # (same geometry) start from its result.
+    tuning = m.autotune(max_group=16) if args.autotune else None
     if args.group:
         m.set_group(args.group)
     group = m.get_tuning("group")
@@ -351,6 +354,8 @@ def run_native(args):
         "config": {"workload": "batched B=128 exact negacyclic products, N=65536 W=1747 L=55 P=114, one q, "
                                "one CUDA graph per step",
                    "global_batch": B * world, "per_gpu_batch": B, "group": group,
+                   "tuning": {k: m.get_tuning(k) for k in ("crt_tiles", "row_rows", "row_bits")},
+                   "autotune": tuning,
                    "l2": "inputs larger than L2 (3.7 GB per step), no flush", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": 2 * B * N * L * 4,
                 "d2h_bytes_per_step": B * N * L * 4, "api": "bcg_multiply (host buffers, pinned)"},
@@ -372,11 +377,25 @@ def run_native(args):
         torch.distributed.destroy_process_group()
 
 
+def autotune_geometries(pkg, args, device, geometries):
+    """Runs the autotuner once per geometry; later contexts of it start tuned."""
+    if not args.autotune:
+        return None
+    out = {}
+    for n, w in geometries:
+        m = pkg.Multiplier(n, w, pkg.inputs.modulus(w, 1), device=device)
+        r = m.autotune(max_group=16)
+        out[f"{n}/{w}"] = {k: r[k] for k in ("group", "crt_tiles", "row_rows", "row_bits", "us_per_product_tuned")}
+        m.close()
+    return out
+
+
 def run_uneven(pkg, args, stream, device):
     """96 products in one graph: 58 at N=32768/W=868 and 38 at N=65536/W=1747,
     three seeded moduli per geometry, four distinct operand pairs per modulus."""
     import numpy as np
     import torch
+    tuned = autotune_geometries(pkg, args, device, [(32768, 868), (65536, 1747)])
     batch = pkg.Batch(device)
     keep = []
     total_bytes = 0
@@ -405,7 +424,7 @@ def run_uneven(pkg, args, stream, device):
     batch.close()
     return {"workload": "96 products: 58 at N=32768/W=868, 38 at N=65536/W=1747, 3 moduli per geometry, "
                         "one CUDA graph per step, device-resident",
-            "products_per_s": 96 / (ms / 1000.0), "ms_per_step": ms, "groups": info["groups"],
+            "products_per_s": 96 / (ms / 1000.0), "ms_per_step": ms, "groups": info["groups"], "autotune": tuned,
             "chains": info["chains"], "launches": info["launches"], "io_bytes": total_bytes}
 
 
@@ -417,6 +436,7 @@ def run_served(pkg, args, device, batched_value):
     import numpy as np
     import torch
     rng = np.random.default_rng(77)
+    autotune_geometries(pkg, args, device, [(16384, 434), (32768, 868), (65536, 1747)])
     srv = pkg.Server(device, slots=3)
     mix = [((16384, 434), 0.3, 1), ((32768, 868), 0.4, 2), ((65536, 1747), 0.3, 2)]
     points = []   # (n, w, q, pid, a pool, b pool, resident ids, out ring)
@@ -555,6 +575,7 @@ def main():
     ap.add_argument("--profile-every", type=int, default=2,
                     help="time the stages of every k-th launch chain with CUDA events")
     ap.add_argument("--no-uneven", dest="uneven", action="store_false", help="skip the uneven 96-product batch")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="keep the default kernel shapes")
     ap.add_argument("--no-served", dest="served", action="store_false", help="skip the served sweep")
     ap.add_argument("--served-loads", default="0.25,0.5,0.75,0.9",
                     help="offered loads as fractions of the estimated capacity")

@@ -99,12 +99,19 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
         if (k == "group") {
             require(value >= 1 && value <= 4096, "group must be in [1, 4096]");
             c.set_group(uint32_t(value));
-        } else if (k == "encode_bstages") {
-            require(value == 2 || value == 3, "encode_bstages must be 2 or 3");
-            c.encode_tuning().bstages = uint32_t(value);
-        } else if (k == "encode_accbuf") {
-            require(value == 2 || value == 4, "encode_accbuf must be 2 or 4");
-            c.encode_tuning().accbuf = uint32_t(value);
+        } else if (k == "crt_tiles") {
+            require(value == 1 || value == 2, "crt_tiles must be 1 or 2");
+            bcg::Tuning t = c.tuning();
+            t.crt_tiles = uint32_t(value);
+            c.set_tuning(t);
+        } else if (k == "row_bits") {
+            require(value >= 0 && value <= 8, "row_bits must be in [0, 8]");
+            c.set_row_bits(uint32_t(value));
+        } else if (k == "row_rows") {
+            require(value >= 0 && value <= 4096, "row_rows must be in [0, 4096]");
+            bcg::Tuning t = c.tuning();
+            t.row_rows = uint32_t(value);
+            c.set_tuning(t);
         } else {
             throw std::invalid_argument("unknown tuning knob: " + k);
         }
@@ -117,9 +124,22 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         const std::string k(knob);
         auto& c = *ctx->ctx;
         if (k == "group") *value = c.group();
-        else if (k == "encode_bstages") *value = c.encode_tuning().bstages;
-        else if (k == "encode_accbuf") *value = c.encode_tuning().accbuf;
+        else if (k == "crt_tiles") *value = c.tuning().crt_tiles;
+        else if (k == "row_rows") *value = c.tuning().row_rows;
+        else if (k == "row_bits") *value = c.geom().r_bits;
         else throw std::invalid_argument("unknown tuning knob: " + k);
+    });
+}
+
+int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_report* out) {
+    return guarded([&] {
+        require(ctx && out, "null argument");
+        const bcg::AutotuneReport r = bcg::autotune(*ctx->ctx, max_group);
+        std::memset(out, 0, sizeof *out);
+        out->group = r.group; out->crt_tiles = r.crt_tiles; out->row_rows = r.row_rows; out->row_bits = r.row_bits;
+        out->candidates = r.candidates;
+        out->us_per_product_default = r.us_per_product_default;
+        out->us_per_product_tuned = r.us_per_product_tuned;
     });
 }
 

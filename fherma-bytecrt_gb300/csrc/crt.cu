@@ -29,13 +29,19 @@
 namespace bcg {
 namespace {
 
+// A CTA covers TILES M tiles of 128 coefficient rows: with 2 tiles every
+// staged weight-digit chunk feeds two MMAs (half the L2 traffic for B); with
+// 1 tile a CTA needs half the TMEM and shared memory, so two CTAs share an SM
+// and one's epilogue overlaps the other's MMA loop.
 constexpr uint32_t kTileRows = 128;
-constexpr uint32_t kTiles = 2;
-constexpr uint32_t kRows = kTileRows * kTiles;
-constexpr uint32_t kProdWarps = 8;
-constexpr uint32_t kCrtThreads = (kProdWarps + 1) * 32;
 constexpr uint32_t kTermsPerChunk = kCrtChunkK / 4;      // 8
 constexpr uint32_t kStages = 4;
+template <int TILES> struct CrtShape {
+    static constexpr uint32_t kRows = kTileRows * TILES;
+    static constexpr uint32_t kProdWarps = 4 * TILES;
+    static constexpr uint32_t kThreads = (kProdWarps + 1) * 32;
+    static constexpr uint32_t kMinBlocks = TILES == 1 ? 2 : 1;
+};
 
 struct CrtSmem {
     uint64_t afull[kStages], bfull[kStages], sempty[kStages], accfull;
@@ -135,21 +141,30 @@ __device__ __forceinline__ void crt_row_epilogue(const CrtArgs& a, uint32_t tadd
     if constexpr (LT > 0) {
         uint32_t z[LT];
         constexpr uint32_t NB = (4 * LT + 1 + 31) / 32;
+        // Double-buffered TMEM reads: batch cb+1 is in flight while batch cb
+        // goes through the carry chain.
+        uint32_t ra[32], rb[32];
+        tmem_ld32_issue(taddr, ra);
+        tmem_ld32_wait(ra);
 #pragma unroll
         for (uint32_t cb = 0; cb < NB; ++cb) {
-            float v[32];
-            tmem_ld32(taddr + cb * 32, v);
+            uint32_t (&cur)[32] = (cb & 1) ? rb : ra;
+            uint32_t (&nxt)[32] = (cb & 1) ? ra : rb;
+            if (cb + 1 < NB) tmem_ld32_issue(taddr + (cb + 1) * 32, nxt);
 #pragma unroll
             for (uint32_t q4 = 0; q4 < 8; ++q4) {
                 const uint32_t l = cb * 8 + q4;
                 if (l < LT) {
-                    const int64_t sum = limb_value(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3], narrow) + carry;
+                    const int64_t sum = limb_value(__uint_as_float(cur[4 * q4]), __uint_as_float(cur[4 * q4 + 1]),
+                                                   __uint_as_float(cur[4 * q4 + 2]), __uint_as_float(cur[4 * q4 + 3]),
+                                                   narrow) + carry;
                     z[l] = uint32_t(sum);
                     carry = sum >> 32;
                 } else if (l == LT && extra) {
-                    carry += int64_t(__float2int_rn(v[4 * q4]));
+                    carry += int64_t(__float2int_rn(__uint_as_float(cur[4 * q4])));
                 }
             }
+            if (cb + 1 < NB) tmem_ld32_wait(nxt);
         }
         if (valid) reduce_mod_q<LT>(z, carry, a, L);
 #pragma unroll
@@ -175,9 +190,12 @@ __device__ __forceinline__ void crt_row_epilogue(const CrtArgs& a, uint32_t tadd
     }
 }
 
-template <int LT>
-__global__ void __launch_bounds__(kCrtThreads, 1)
+template <int LT, int TILES>
+__global__ void __launch_bounds__(CrtShape<TILES>::kThreads, CrtShape<TILES>::kMinBlocks)
 crt_kernel(const __grid_constant__ CrtArgs a) {
+    constexpr uint32_t kTiles = TILES;
+    constexpr uint32_t kRows = CrtShape<TILES>::kRows;
+    constexpr uint32_t kProdWarps = CrtShape<TILES>::kProdWarps;
     extern __shared__ __align__(1024) uint8_t smem[];
     const uint32_t NC = a.NC;
     const uint32_t a_bytes = kRows * kCrtChunkK * 2;              // both tiles
@@ -210,10 +228,10 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
         ctl->abort_flag = 0;
         mbar_fence_init();
     }
-    // Two tile accumulators of NC fp32 columns each.
+    // One accumulator of NC fp32 columns per tile.
     const uint32_t tile_cols = NC <= 128 ? 128u : 256u;
     if (warp == kProdWarps) {
-        tmem_alloc(&ctl->tmem_base, 2 * tile_cols);
+        tmem_alloc(&ctl->tmem_base, kTiles * tile_cols);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -265,7 +283,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
         }
         __syncwarp();
     } else {
-        const uint32_t r = threadIdx.x;                    // 0..255
+        const uint32_t r = threadIdx.x;                    // 0..kRows-1
         const uint32_t tile = r / kTileRows, trow = r % kTileRows;
         const bool valid = r < rows;
         float acc = 0.0f;
@@ -288,7 +306,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
 #pragma unroll
             for (uint32_t jj = 0; jj < kTermsPerChunk; ++jj) {
                 const uint32_t u = kc * kTermsPerChunk + jj;
-                if (u < P) acc = __fadd_rn(acc, __fmul_rn(__uint2float_rn(t[jj]), __ldg(a.invp + u)));
+                if (u < P) acc = __fadd_rn(acc, __fmul_rn(__uint2float_rn(t[jj]), a.invp[u]));
                 else if (u == P) t[jj] = __float2uint_rn(acc);
             }
 #pragma unroll
@@ -331,34 +349,43 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
     __syncthreads();
     if (warp == kProdWarps) {
         tc_fence_after();
-        tmem_dealloc(tmem, 2 * tile_cols);
+        tmem_dealloc(tmem, kTiles * tile_cols);
     }
 }
 
 }  // namespace
 
-size_t crt_smem_bytes(uint32_t NC) {
-    const size_t stage = size_t(kRows) * kCrtChunkK * 2 + size_t(NC) * kCrtChunkK * 2 + kTermsPerChunk * kRows * 4;
+size_t crt_smem_bytes(uint32_t NC, uint32_t tiles) {
+    const size_t rows = size_t(kTileRows) * tiles;
+    const size_t stage = rows * kCrtChunkK * 2 + size_t(NC) * kCrtChunkK * 2 + kTermsPerChunk * rows * 4;
     return kStages * stage + sizeof(CrtSmem) + 1024;
 }
 
-template <int LT>
+template <int LT, int TILES>
 static cudaError_t launch_crt_t(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
-    const size_t smem = crt_smem_bytes(a.NC);
-    cudaError_t e = cudaFuncSetAttribute(crt_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    const size_t smem = crt_smem_bytes(a.NC, TILES);
+    cudaError_t e = cudaFuncSetAttribute(crt_kernel<LT, TILES>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    const dim3 grid((a.N + kRows - 1) / kRows, nprod);
-    crt_kernel<LT><<<grid, kCrtThreads, smem, st>>>(a);
+    constexpr uint32_t rows = CrtShape<TILES>::kRows;
+    const dim3 grid((a.N + rows - 1) / rows, nprod);
+    crt_kernel<LT, TILES><<<grid, CrtShape<TILES>::kThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
+template <int TILES>
+static cudaError_t launch_crt_tiles(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
     switch (a.L) {
-        case 14: return launch_crt_t<14>(a, nprod, st);
-        case 28: return launch_crt_t<28>(a, nprod, st);
-        case 55: return launch_crt_t<55>(a, nprod, st);
-        default: return launch_crt_t<0>(a, nprod, st);
+        case 14: return launch_crt_t<14, TILES>(a, nprod, st);
+        case 28: return launch_crt_t<28, TILES>(a, nprod, st);
+        case 55: return launch_crt_t<55, TILES>(a, nprod, st);
+        default: return launch_crt_t<0, TILES>(a, nprod, st);
     }
+}
+
+cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st, uint32_t tiles) {
+    if (tiles == 1) return launch_crt_tiles<1>(a, nprod, st);
+    if (tiles == 2) return launch_crt_tiles<2>(a, nprod, st);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace bcg

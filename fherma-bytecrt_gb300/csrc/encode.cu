@@ -308,8 +308,7 @@ static cudaError_t launch_encode_t(EncodeArgs a, uint32_t nprod, cudaStream_t st
     return cudaGetLastError();
 }
 
-cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands,
-                          const EncodeTuning&) {
+cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands) {
     switch (a.L) {
         case 14: return launch_encode_t<14>(a, nprod, st, operands);
         case 28: return launch_encode_t<28>(a, nprod, st, operands);

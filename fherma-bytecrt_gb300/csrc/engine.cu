@@ -32,8 +32,8 @@ void parallel_copy(void* dst, const void* src, size_t bytes) {
 std::shared_ptr<const GeometryTables> geometry_tables(int device, const HostPlan& plan) {
     // Weak entries: the tables live as long as some Context of the geometry does.
     static std::mutex mu;
-    static std::map<std::tuple<int, uint32_t, uint32_t, uint32_t>, std::weak_ptr<const GeometryTables>> cache;
-    const auto key = std::make_tuple(device, plan.g.N, plan.g.W, plan.g.L);
+    static std::map<std::tuple<int, uint32_t, uint32_t, uint32_t, uint32_t>, std::weak_ptr<const GeometryTables>> cache;
+    const auto key = std::make_tuple(device, plan.g.N, plan.g.W, plan.g.L, plan.g.R);
     std::lock_guard<std::mutex> lock(mu);
     if (auto hit = cache[key].lock()) return hit;
     auto t = std::make_shared<GeometryTables>();
@@ -44,7 +44,6 @@ std::shared_ptr<const GeometryTables> geometry_tables(int device, const HostPlan
     upload(t->consts, plan.prime_consts.data(), plan.prime_consts.size() * 4);
     upload(t->tables, plan.ntt_tables.data(), plan.ntt_tables.size() * 4);
     upload(t->enc_b, plan.enc_b.data(), plan.enc_b.size() * 2);
-    upload(t->invp, plan.invp.data(), plan.invp.size() * 4);
     cache[key] = t;
     return t;
 }
@@ -74,15 +73,7 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     status_.allocate(16);
     check(cudaMemset(status_.ptr, 0, 16), "status reset");
 
-    const TableOffsets off = table_offsets(g);
-    ntt_.consts = geo_->consts.as<uint4>();
-    ntt_.tables = geo_->tables.as<uint2>();
-    ntt_.table_stride = g.table_stride;
-    ntt_.off_col_f = off.col_f; ntt_.off_col_i = off.col_i;
-    ntt_.off_row_f = off.row_f; ntt_.off_row_i = off.row_i;
-    ntt_.off_tw_lo = off.tw_lo; ntt_.off_tw_hi = off.tw_hi;
-    ntt_.off_itw_lo = off.itw_lo; ntt_.off_itw_hi = off.itw_hi;
-    ntt_.N = g.N; ntt_.P = g.P; ntt_.c_bits = g.c_bits; ntt_.z_bits = g.z_bits; ntt_.Z = g.Z; ntt_.H = g.H;
+    bind_ntt();
 
     enc_.enc_b = geo_->enc_b.as<uint16_t>();
     for (uint32_t j = 0; j < g.P; ++j)
@@ -91,7 +82,7 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     enc_.status = status_.as<uint32_t>();
 
     crt_.crt_b = crt_b_.as<uint16_t>();
-    crt_.invp = geo_->invp.as<float>();
+    for (uint32_t j = 0; j < g.P; ++j) crt_.invp[j] = plan_.invp[j];
     for (uint32_t l = 0; l < g.L; ++l) crt_.q[l] = plan_.q[l];
     crt_.q_inv_scaled = plan_.q_inv_scaled;
     crt_.N = g.N; crt_.L = g.L; crt_.P = g.P; crt_.k_total = g.crt_k_total; crt_.kchunks = g.crt_kchunks;
@@ -101,6 +92,9 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     // Products per launch chain: long chains amortise each kernel's launch and
     // tail (8 products per chain at N=65536 measured 16% faster than 1).
     group_ = std::min<uint32_t>(256, std::max<uint32_t>(1, 524288 / g.N));
+    // A geometry the autotuner already measured in this process starts tuned.
+    AutotuneReport tuned;
+    if (cached_autotune(device_, g.N, g.W, g.L, &tuned)) apply_autotune(*this, tuned);
 }
 
 Context::~Context() {
@@ -117,7 +111,43 @@ Context::~Context() {
     if (stream_) cudaStreamDestroy(stream_);
 }
 
+void Context::bind_ntt() {
+    const Geometry& g = plan_.g;
+    const TableOffsets off = table_offsets(g);
+    const uint32_t row_rows = ntt_.row_rows;
+    ntt_ = NttArgs{};
+    ntt_.consts = geo_->consts.as<uint4>();
+    ntt_.tables = geo_->tables.as<uint2>();
+    ntt_.table_stride = g.table_stride;
+    ntt_.off_col_f = off.col_f; ntt_.off_col_i = off.col_i;
+    ntt_.off_row_f = off.row_f; ntt_.off_row_i = off.row_i;
+    ntt_.off_tw_lo = off.tw_lo; ntt_.off_tw_hi = off.tw_hi;
+    ntt_.off_itw_lo = off.itw_lo; ntt_.off_itw_hi = off.itw_hi;
+    ntt_.N = g.N; ntt_.P = g.P; ntt_.c_bits = g.c_bits; ntt_.z_bits = g.z_bits; ntt_.Z = g.Z; ntt_.H = g.H;
+    ntt_.R = g.R;
+    ntt_.row_rows = row_rows;
+}
+
+void Context::set_row_bits(uint32_t row_bits) {
+    // Only the NTT tables depend on the split; the encode and CRT operands stay.
+    HostPlan p = make_plan(plan_.g.N, plan_.g.W, plan_.g.L, plan_.q.data(), row_bits);
+    // The old tables may be freed below: no launch on any stream may still read them.
+    check(cudaDeviceSynchronize(), "device synchronize");
+    auto geo = geometry_tables(device_, p);
+    plan_ = std::move(p);
+    geo_ = std::move(geo);
+    enc_.enc_b = geo_->enc_b.as<uint16_t>();
+    bind_ntt();
+}
+
 void Context::set_group(uint32_t g) { group_ = std::max<uint32_t>(1, g); }
+
+void Context::set_tuning(const Tuning& t) {
+    if (t.crt_tiles != 1 && t.crt_tiles != 2) throw std::invalid_argument("crt_tiles must be 1 or 2");
+    if (t.row_rows > 4096) throw std::invalid_argument("row_rows must be at most 4096");
+    tuning_ = t;
+    ntt_.row_rows = t.row_rows;
+}
 
 void Context::ensure_workspace(uint32_t products) {
     if (products <= ws_products_) return;
@@ -181,7 +211,7 @@ void Context::encode(const uint32_t* a, const uint32_t* b, uint32_t* pa, uint32_
     EncodeArgs e = enc_;
     e.in0 = a; e.in1 = b; e.in_stride = coeff_words();
     e.out0 = pa; e.out1 = pb; e.out_stride = plane_stride;
-    check(launch_encode(e, count, st, 2, enc_tuning_), "encode launch");
+    check(launch_encode(e, count, st, 2), "encode launch");
 }
 
 void Context::negacyclic(uint32_t* pa, uint32_t* pb, size_t plane_stride, uint32_t count, cudaStream_t st) {
@@ -196,7 +226,7 @@ void Context::crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint3
     CrtArgs a = crt_;
     a.terms = terms; a.terms_stride = plane_stride;
     a.out = c; a.out_stride = coeff_words();
-    check(launch_crt(a, count, st), "CRT launch");
+    check(launch_crt(a, count, st, tuning_.crt_tiles), "CRT launch");
 }
 
 void Context::mark_begin(int stage, cudaStream_t st) {
@@ -286,7 +316,7 @@ void Context::forward_spectral(const uint32_t* x, uint32_t* planes, cudaStream_t
     EncodeArgs e = enc_;
     e.in0 = x; e.in1 = x; e.in_stride = 0;
     e.out0 = planes; e.out1 = planes; e.out_stride = 0;
-    check(launch_encode(e, 1, st, 1, enc_tuning_), "encode launch");
+    check(launch_encode(e, 1, st, 1), "encode launch");
     check(launch_col_forward(ntt_, planes, 0, 1, st), "column pass launch");
     check(launch_row_forward(ntt_, planes, 0, 1, st), "row forward launch");
 }
@@ -297,7 +327,7 @@ void Context::multiply_spectral_device(const uint32_t* a_spectral, const uint32_
     EncodeArgs e = enc_;
     e.in0 = b; e.in1 = b; e.in_stride = coeff_words();
     e.out0 = ws; e.out1 = ws; e.out_stride = pw;
-    check(launch_encode(e, count, st, 1, enc_tuning_), "encode launch");
+    check(launch_encode(e, count, st, 1), "encode launch");
     check(launch_col_forward(ntt_, ws, pw, count, st), "column pass launch");
     check(launch_row_product(ntt_, a_spectral, 0, ws, pw, ws, pw, count, true, st), "row pass launch");
     check(launch_col_inverse(ntt_, ws, pw, count, st), "inverse column pass launch");

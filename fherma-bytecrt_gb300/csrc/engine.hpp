@@ -71,11 +71,11 @@ struct PinnedBuffer {
 };
 
 // Device tables that depend only on the geometry (N, W, L) and the device:
-// prime constants, NTT twiddle/twist tables, the encode B operand and 1/p_j.
+// prime constants, NTT twiddle/twist tables and the encode B operand.
 // Every Context of the same geometry on a device shares one copy (moduli of a
 // geometry differ only in the CRT weights and q, which stay per Context).
 struct GeometryTables {
-    DeviceBuffer consts, tables, enc_b, invp;
+    DeviceBuffer consts, tables, enc_b;
 };
 std::shared_ptr<const GeometryTables> geometry_tables(int device, const HostPlan& plan);
 
@@ -129,8 +129,10 @@ public:
                StageTimer* timer = nullptr);
 
     NttArgs ntt_args() const { return ntt_; }
-    EncodeTuning& encode_tuning() { return enc_tuning_; }
-    const EncodeTuning& encode_tuning() const { return enc_tuning_; }
+    const Tuning& tuning() const { return tuning_; }
+    void set_tuning(const Tuning& t);
+    // NTT split N = C * 2^row_bits (0: the default R = min(N, 256)); re-plans the NTT tables.
+    void set_row_bits(uint32_t row_bits);
 
     // Per-stage timing with CUDA events recorded on the launching stream.
     enum Stage { kEncode = 0, kColForward, kRow, kColInverse, kCrt, kStages };
@@ -156,6 +158,7 @@ private:
     void ensure_device_io(uint32_t products);
     void ensure_host_staging(uint32_t products);
     void multiply_pinned(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
+    void bind_ntt();
 
     HostPlan plan_;
     int device_ = 0;
@@ -174,8 +177,18 @@ private:
     NttArgs ntt_{};
     EncodeArgs enc_{};
     CrtArgs crt_{};
-    EncodeTuning enc_tuning_{};
+    Tuning tuning_{};
 };
+
+// Autotuner (autotune.cu): times candidate shapes for ctx's geometry, applies
+// the fastest and records it for later Contexts of the same geometry.
+struct AutotuneReport {
+    uint32_t group = 0, crt_tiles = 0, row_rows = 0, row_bits = 0, candidates = 0;
+    double us_per_product_default = 0, us_per_product_tuned = 0;
+};
+AutotuneReport autotune(Context& ctx, uint32_t max_group);
+bool cached_autotune(int device, uint32_t N, uint32_t W, uint32_t L, AutotuneReport* out);
+void apply_autotune(Context& ctx, const AutotuneReport& r);
 
 // Thread-local last error message for the C ABI.
 void set_last_error(const std::string& msg);

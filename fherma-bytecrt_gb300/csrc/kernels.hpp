@@ -34,29 +34,29 @@ struct CrtArgs {
     uint32_t* out;           // [N][L] canonical limbs
     size_t out_stride;
     const uint16_t* crt_b;   // fp16 weight-digit matrix, chunked over K
-    const float* invp;
     double q_inv_scaled;
     uint32_t N, L, P, k_total, kchunks, E, NC;
     uint32_t* status;
     uint32_t q[kMaxLimbs];
+    float invp[256];         // float(1/p_j): warp-uniform reads from the constant cache
 };
 
 struct NttArgs;   // ntt.cuh
 
 // Encode pipeline knobs: B-operand stages (2 or 3) and TMEM chunk buffers (2 or 4).
-struct EncodeTuning {
-    uint32_t bstages = 2;
-    uint32_t accbuf = 4;
+// Kernel shape knobs (the autotuner's search space, bcg_context_set_tuning).
+struct Tuning {
+    uint32_t crt_tiles = 2;   // 128-row M tiles per CRT CTA: 2 (shared B chunks) or 1 (two CTAs per SM)
+    uint32_t row_rows = 0;    // rows of the row pass per CTA; 0: up to 32
 };
 
 size_t encode_smem_bytes(uint32_t K, uint32_t group_cols);
 uint32_t encode_group_cols(uint32_t cols, uint32_t K);
-size_t crt_smem_bytes(uint32_t NC);
+size_t crt_smem_bytes(uint32_t NC, uint32_t tiles);
 
 // Encodes operand A (and operand B when operands == 2) of nprod products (grid.y = operand).
-cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands = 2,
-                          const EncodeTuning& tuning = EncodeTuning());
-cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st);
+cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands = 2);
+cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st, uint32_t tiles = 2);
 
 // Column passes over nplanes prime-plane sets, set z at planes + z*stride.
 cudaError_t launch_col_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st);

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(32 * ((1 << CB) >> local_bits(CB)))
 col_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride) {
     constexpr int LOCAL = local_bits(CB);
     constexpr int NPH = phase_count(CB);
-    constexpr uint32_t R = 256;
+    const uint32_t R = a.R;                 // column stride: the row length
     __shared__ uint32_t buf[(1 << CB) * 32];
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t j = blockIdx.y;
@@ -262,9 +262,9 @@ row_forward_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride
 // ---------------------------------------------------------------- launchers --
 template <bool INVERSE>
 static cudaError_t launch_col(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
-    const uint32_t C = a.N / 256;
+    const uint32_t C = a.N / a.R;
     if (C <= 1) return cudaSuccess;
-    const dim3 grid(256 / 32, a.P, nplanes);
+    const dim3 grid(a.R / 32, a.P, nplanes);
     switch (a.c_bits) {
 #define BCG_COL(CBV) case CBV: col_kernel<CBV, INVERSE><<<grid, 32 * ((1 << CBV) >> local_bits(CBV)), 0, st>>>(a, planes, stride); break;
         BCG_COL(1) BCG_COL(2) BCG_COL(3) BCG_COL(4) BCG_COL(5) BCG_COL(6) BCG_COL(7) BCG_COL(8)
@@ -281,14 +281,15 @@ cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride
     return launch_col<true>(a, planes, stride, nplanes, st);
 }
 
-static uint32_t row_rows_per_cta(uint32_t C, uint32_t rows_per_iter) {
-    uint32_t rows = C < 32 ? C : 32;
+static uint32_t row_rows_per_cta(uint32_t C, uint32_t rows_per_iter, uint32_t wanted) {
+    uint32_t rows = wanted ? wanted : 32;
+    if (rows > C) rows = C;
     if (rows < rows_per_iter) rows = rows_per_iter;
     return rows;
 }
 
 size_t row_smem_bytes(const NttArgs& a, bool forward_only) {
-    const uint32_t R = a.N < 256 ? a.N : 256;
+    const uint32_t R = a.R;
     const size_t tabs = forward_only ? (R + a.Z + a.H) : (2 * R + 2 * a.Z + 2 * a.H);
     return tabs * sizeof(uint2) + (forward_only ? 1 : 2) * kRowWarps * 256 * sizeof(uint32_t);
 }
@@ -296,10 +297,10 @@ size_t row_smem_bytes(const NttArgs& a, bool forward_only) {
 cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_t a_stride,
                                const uint32_t* planes_b, size_t b_stride, uint32_t* planes_out,
                                size_t out_stride, uint32_t nprod, bool a_spectral, cudaStream_t st) {
-    const uint32_t R = a.N < 256 ? a.N : 256;
+    const uint32_t R = a.R;
     const uint32_t C = a.N / R;
     const uint32_t rpi = kRowWarps * (32 / (R / 8));
-    const uint32_t rows = row_rows_per_cta(C, rpi);
+    const uint32_t rows = row_rows_per_cta(C, rpi, a.row_rows);
     const dim3 grid((C + rows - 1) / rows, a.P, nprod);
     const size_t smem = row_smem_bytes(a, false);
     const uint32_t rb = 31 - __builtin_clz(R);
@@ -315,10 +316,10 @@ cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_
 }
 
 cudaError_t launch_row_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
-    const uint32_t R = a.N < 256 ? a.N : 256;
+    const uint32_t R = a.R;
     const uint32_t C = a.N / R;
     const uint32_t rpi = kRowWarps * (32 / (R / 8));
-    const uint32_t rows = row_rows_per_cta(C, rpi);
+    const uint32_t rows = row_rows_per_cta(C, rpi, a.row_rows);
     const dim3 grid((C + rows - 1) / rows, a.P, nplanes);
     const size_t smem = row_smem_bytes(a, true);
     const uint32_t rb = 31 - __builtin_clz(R);

@@ -32,6 +32,8 @@ struct NttArgs {
     uint32_t off_col_f, off_col_i, off_row_f, off_row_i;
     uint32_t off_tw_lo, off_tw_hi, off_itw_lo, off_itw_hi;
     uint32_t N, P, c_bits, z_bits, Z, H;
+    uint32_t R;                // row length of the split N = C * R
+    uint32_t row_rows;         // rows of the row pass per CTA (0: up to 32)
 };
 
 // Bit positions handled inside one thread during phase `phase` of a transform

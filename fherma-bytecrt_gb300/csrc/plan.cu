@@ -190,7 +190,7 @@ TableOffsets table_offsets(const Geometry& g) {
     return o;
 }
 
-HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw) {
+HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw, uint32_t row_bits) {
     if (N < 16 || N > 65536 || (N & (N - 1)))
         throw std::invalid_argument("N must be a power of two in [16, 65536]");
     if (W < 2 || L != (W + 31) / 32)
@@ -205,7 +205,9 @@ HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw) {
     Geometry& g = plan.g;
     g.N = N; g.W = W; g.L = L;
     g.n_bits = 31 - __builtin_clz(N);
-    g.R = std::min<uint32_t>(N, 256);
+    g.R = row_bits ? (1u << row_bits) : std::min<uint32_t>(N, 256);
+    if (row_bits > 8 || g.R > N || g.R < 16 || N / g.R > 256 || (N / g.R > 1 && g.R < 32))
+        throw std::invalid_argument("row_bits gives an unsupported NTT split for this N");
     g.C = N / g.R;
     g.r_bits = 31 - __builtin_clz(g.R);
     g.c_bits = 31 - __builtin_clz(g.C);

@@ -50,8 +50,10 @@ struct TableOffsets {
 };
 TableOffsets table_offsets(const Geometry& g);
 
-// Throws std::invalid_argument for an unsupported point.
-HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q);
+// Throws std::invalid_argument for an unsupported point.  row_bits picks the
+// NTT split N = C * R with R = 2^row_bits (0: R = min(N, 256)); it needs
+// C <= 256, 16 <= R <= 256, and R >= 32 when C > 1.
+HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, uint32_t row_bits = 0);
 
 uint32_t bit_reverse(uint32_t x, uint32_t bits);
 

@@ -43,6 +43,12 @@ class bcg_profile(ctypes.Structure):
                 ("chains", ctypes.c_uint64)]
 
 
+class bcg_autotune_report(ctypes.Structure):
+    _fields_ = [("group", ctypes.c_uint32), ("crt_tiles", ctypes.c_uint32), ("row_rows", ctypes.c_uint32),
+                ("row_bits", ctypes.c_uint32), ("candidates", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("us_per_product_default", ctypes.c_double), ("us_per_product_tuned", ctypes.c_double)]
+
+
 class bcg_batch_info(ctypes.Structure):
     _fields_ = [("groups", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("products", ctypes.c_uint64),
                 ("chains", ctypes.c_uint64), ("launches", ctypes.c_uint64)]
@@ -92,6 +98,7 @@ def lib():
         L.bcg_context_set_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
         L.bcg_context_get_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.bcg_multiply.argtypes = [vp, _u32p, _u32p, _u32p, ctypes.c_uint32]
+        L.bcg_context_autotune.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(bcg_autotune_report)]
         L.bcg_multiply_device.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
         L.bcg_multiply_device_static.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
         L.bcg_encode_device.argtypes = [vp, vp, vp, vp, vp, ctypes.c_size_t, ctypes.c_uint32, vp]
@@ -221,6 +228,12 @@ class Multiplier:
         return int(v.value)
 
     # ---- host buffers
+    def autotune(self, max_group: int = 16) -> dict:
+        """Times candidate kernel shapes for this geometry and keeps the fastest."""
+        r = bcg_autotune_report()
+        _check(lib().bcg_context_autotune(self._h, max_group, ctypes.byref(r)))
+        return {n: getattr(r, n) for n, _ in bcg_autotune_report._fields_ if n != "reserved"}
+
     def multiply(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
         a = np.ascontiguousarray(a, dtype=np.uint32)
         b = np.ascontiguousarray(b, dtype=np.uint32)

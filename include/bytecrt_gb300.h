@@ -73,11 +73,27 @@ int bcg_context_info(const bcg_context* ctx, bcg_info* out);
  * GPU for the point; the autotuner may change it. */
 int bcg_context_set_group(bcg_context* ctx, uint32_t group);
 /* Kernel shape knobs (the autotuner's search space), by name:
- *   "group"           products per launch chain, 1..4096
- *   "encode_bstages"  B-operand shared-memory stages of the encode MMA loop, 2 or 3
- *   "encode_accbuf"   TMEM accumulator buffers of the encode kernel, 2 or 4 */
+ *   "group"      products per launch chain, 1..4096
+ *   "crt_tiles"  CRT MMA tile shape: 128-row M tiles per CTA, 2 (each staged
+ *                weight-digit chunk feeds both) or 1 (two CTAs per SM)
+ *   "row_rows"   rows per row-pass CTA; 0: up to 32
+ *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
+ *                Re-plans the twiddle and twist tables (the primes stay). */
 int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value);
 int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* value);
+/* Autotuner: times whole launch chains on synthetic operands for every value
+ * of row_bits, then crt_tiles, row_rows and group (coordinate search, at most
+ * max_group products per chain and 4 GB of workspace), keeps the fastest, and
+ * records it so that contexts of the same geometry created later in the
+ * process (including those of bcg_batch and bcg_server) start from it.  The
+ * reference fixes these shapes per geometry at compile time. */
+typedef struct bcg_autotune_report {
+    uint32_t group, crt_tiles, row_rows, row_bits;
+    uint32_t candidates;    /* settings timed */
+    uint32_t reserved;
+    double us_per_product_default, us_per_product_tuned;
+} bcg_autotune_report;
+int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_report* out);
 
 /* ---- whole products.
  * bcg_multiply: host buffers, synchronous; replaces fherma_run

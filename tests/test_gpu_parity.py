@@ -175,3 +175,74 @@ def test_plugin_abi_roundtrip():
     with pytest.raises(RuntimeError):
         pkg.fherma_run(st, pkg.Inputs(a=a[:-1], b=b))
     pkg.fherma_free(st)
+
+
+@pytest.mark.parametrize("N,W", [(64, 100), (2048, 300), (16384, 434), (65536, 1747)])
+def test_tuning_knobs_stay_bit_exact(N, W):
+    """Every CRT tile shape and row-pass CTA shape gives the oracle's product."""
+    pkg = package()
+    m, o, q = setup(N, W, 1)
+    a = np.stack([pkg.inputs.uniform(q, N, 70 + i) for i in range(3)])
+    b = np.stack([pkg.inputs.uniform(q, N, 80 + i) for i in range(3)])
+    want = [o.multiply(a[i], b[i]) for i in range(3)]
+    da, db = dev(a), dev(b)
+    for tiles in (1, 2):
+        for rows in (0, 8, 64):
+            m.set_tuning("crt_tiles", tiles)
+            m.set_tuning("row_rows", rows)
+            out = torch.zeros_like(da)
+            m.multiply_device(da, db, out, 3)
+            m.synchronize()
+            for i in range(3):
+                assert np.array_equal(host(out[i]), want[i]), (tiles, rows, i)
+    m.set_tuning("crt_tiles", 2)
+    m.set_tuning("row_rows", 0)
+
+
+@pytest.mark.parametrize("N,W", [(1024, 200), (4096, 868), (32768, 868)])
+def test_radix_splits_stay_bit_exact(N, W):
+    """Every valid split N = C * 2^row_bits gives the oracle's product."""
+    pkg = package()
+    q = pkg.inputs.modulus(W, 21)
+    o = O.Oracle(N, W, q)
+    a, b = pkg.inputs.uniform(q, N, 1), pkg.inputs.uniform(q, N, 2)
+    want = o.multiply(a, b)
+    m = pkg.Multiplier(N, W, q)
+    n_bits = N.bit_length() - 1
+    tried = 0
+    for rb in range(max(4, n_bits - 8), min(8, n_bits) + 1):
+        if N >> rb > 1 and rb < 5:
+            continue
+        m.set_tuning("row_bits", rb)
+        assert m.get_tuning("row_bits") == rb
+        out = torch.zeros((1, N, len(q)), dtype=torch.int32, device="cuda")
+        m.multiply_device(dev(a[None]), dev(b[None]), out, 1)
+        m.synchronize()
+        assert np.array_equal(host(out[0]), want), rb
+        tried += 1
+    assert tried >= 2
+    m.close()
+
+
+def test_autotune_applies_and_is_remembered():
+    pkg = package()
+    N, W = 16384, 434
+    q = pkg.inputs.modulus(W, 31)
+    m = pkg.Multiplier(N, W, q)
+    r = m.autotune(max_group=8)
+    assert r["candidates"] >= 5
+    assert 0 < r["us_per_product_tuned"] <= r["us_per_product_default"] * 1.05
+    assert r["crt_tiles"] in (1, 2) and 1 <= r["group"] <= 8
+    for knob in ("group", "crt_tiles", "row_rows", "row_bits"):
+        assert m.get_tuning(knob) == r[knob], knob
+    a, b = pkg.inputs.uniform(q, N, 3), pkg.inputs.uniform(q, N, 4)
+    assert np.array_equal(m.multiply(a, b), O.Oracle(N, W, q).multiply(a, b))
+    # Another context of the same geometry (another q) starts from the tuned shapes.
+    q2 = pkg.inputs.modulus(W, 32)
+    m2 = pkg.Multiplier(N, W, q2)
+    for knob in ("group", "crt_tiles", "row_rows", "row_bits"):
+        assert m2.get_tuning(knob) == r[knob], knob
+    a2, b2 = pkg.inputs.uniform(q2, N, 5), pkg.inputs.uniform(q2, N, 6)
+    assert np.array_equal(m2.multiply(a2, b2), O.Oracle(N, W, q2).multiply(a2, b2))
+    m.close()
+    m2.close()
