@@ -26,9 +26,10 @@ std::map<Key, AutotuneReport>& tuned() {
 }
 
 struct Settings {
-    uint32_t row_bits, crt_tiles, row_rows, group;
+    uint32_t row_bits, crt_tiles, crt_persistent, row_rows, group;
     bool operator==(const Settings& o) const {
-        return row_bits == o.row_bits && crt_tiles == o.crt_tiles && row_rows == o.row_rows && group == o.group;
+        return row_bits == o.row_bits && crt_tiles == o.crt_tiles && crt_persistent == o.crt_persistent &&
+               row_rows == o.row_rows && group == o.group;
     }
 };
 
@@ -36,6 +37,7 @@ void apply(Context& ctx, const Settings& s) {
     if (ctx.geom().r_bits != s.row_bits) ctx.set_row_bits(s.row_bits);
     Tuning t = ctx.tuning();
     t.crt_tiles = s.crt_tiles;
+    t.crt_persistent = s.crt_persistent;
     t.row_rows = s.row_rows;
     ctx.set_tuning(t);
     ctx.set_group(s.group);
@@ -52,7 +54,7 @@ bool cached_autotune(int device, uint32_t N, uint32_t W, uint32_t L, AutotuneRep
 }
 
 void apply_autotune(Context& ctx, const AutotuneReport& r) {
-    apply(ctx, Settings{r.row_bits, r.crt_tiles, r.row_rows, r.group});
+    apply(ctx, Settings{r.row_bits, r.crt_tiles, r.crt_persistent, r.row_rows, r.group});
 }
 
 AutotuneReport autotune(Context& ctx, uint32_t max_group) {
@@ -110,7 +112,8 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
     };
 
     AutotuneReport r{};
-    Settings cur{g0.r_bits, ctx.tuning().crt_tiles, ctx.tuning().row_rows, std::min(ctx.group(), gmax)};
+    Settings cur{g0.r_bits, ctx.tuning().crt_tiles, ctx.tuning().crt_persistent, ctx.tuning().row_rows,
+                 std::min(ctx.group(), gmax)};
     double cur_us = measure(cur);
     r.us_per_product_default = cur_us;
     auto consider = [&](Settings s) {
@@ -128,7 +131,8 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
     for (uint32_t rb = (nb > 8 ? nb - 8 : 4); rb <= std::min<uint32_t>(8, nb); ++rb) {
         Settings s = cur; s.row_bits = rb; consider(s);
     }
-    for (uint32_t t : {2u, 1u}) { Settings s = cur; s.crt_tiles = t; consider(s); }
+    for (uint32_t t : {2u, 1u}) { Settings s = cur; s.crt_persistent = 0; s.crt_tiles = t; consider(s); }
+    { Settings s = cur; s.crt_persistent = 1; consider(s); }
     for (uint32_t rr : {0u, 8u, 16u, 64u, 128u}) { Settings s = cur; s.row_rows = rr; consider(s); }
     for (uint32_t gr : {1u, 2u, 4u, 8u, 16u, 32u}) {
         if (gr > gmax) break;
@@ -139,6 +143,7 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
     check(cudaEventDestroy(e1), "event");
     r.row_bits = cur.row_bits;
     r.crt_tiles = cur.crt_tiles;
+    r.crt_persistent = cur.crt_persistent;
     r.row_rows = cur.row_rows;
     r.group = cur.group;
     r.us_per_product_tuned = cur_us;

@@ -104,6 +104,11 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
             bcg::Tuning t = c.tuning();
             t.crt_tiles = uint32_t(value);
             c.set_tuning(t);
+        } else if (k == "crt_persistent") {
+            require(value == 0 || value == 1, "crt_persistent must be 0 or 1");
+            bcg::Tuning t = c.tuning();
+            t.crt_persistent = uint32_t(value);
+            c.set_tuning(t);
         } else if (k == "row_bits") {
             require(value >= 0 && value <= 8, "row_bits must be in [0, 8]");
             c.set_row_bits(uint32_t(value));
@@ -127,6 +132,7 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         else if (k == "crt_tiles") *value = c.tuning().crt_tiles;
         else if (k == "row_rows") *value = c.tuning().row_rows;
         else if (k == "row_bits") *value = c.geom().r_bits;
+        else if (k == "crt_persistent") *value = c.tuning().crt_persistent;
         else throw std::invalid_argument("unknown tuning knob: " + k);
     });
 }
@@ -138,6 +144,7 @@ int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_repo
         std::memset(out, 0, sizeof *out);
         out->group = r.group; out->crt_tiles = r.crt_tiles; out->row_rows = r.row_rows; out->row_bits = r.row_bits;
         out->candidates = r.candidates;
+        out->crt_persistent = r.crt_persistent;
         out->us_per_product_default = r.us_per_product_default;
         out->us_per_product_tuned = r.us_per_product_tuned;
     });

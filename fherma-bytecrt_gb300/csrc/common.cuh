@@ -153,6 +153,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
     }
 }
 
+// Waits for this thread's own asynchronous work (copies, MMAs) to land before
+// the CTA leaves: bounded by the same limit, but not cut short by the abort
+// flag (an aborted CTA must still not exit with its copies in flight).
+__device__ __forceinline__ bool mbar_wait_own(uint64_t* bar, uint32_t parity, uint32_t* status) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t start = global_ns();
+    for (uint32_t spin = 0;; ++spin) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((spin & 63) == 0 && global_ns() - start > kWaitLimitNs) {
+            atomicExch(status, kStatusWaitTimeout);
+            return false;
+        }
+    }
+}
+
 // ------------------------------------------------------- bulk async copy --
 // 1-D global -> shared copy completing on an mbarrier (transaction bytes).
 // Both addresses 16-byte aligned, bytes a multiple of 16.
@@ -161,6 +176,23 @@ __device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, 
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
         :: "r"(smem_u32(smem_dst)), "l"(gmem_src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+// 1-D shared -> global bulk copy (bulk-group completion).  Both addresses
+// 16-byte aligned, bytes a multiple of 16; the writes to smem_src must be made
+// visible to the async proxy first (fence_proxy_async + a barrier).
+__device__ __forceinline__ void bulk_store(void* gmem_dst, const void* smem_src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                 :: "l"(gmem_dst), "r"(smem_u32(smem_src)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// The sources of this thread's bulk stores have been read (smem reusable).
+__device__ __forceinline__ void bulk_store_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// This thread's bulk stores are complete.
+__device__ __forceinline__ void bulk_store_wait_all() {
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 // Hint: bring [src, src + bytes) into L2 ahead of a later bulk copy.

@@ -144,6 +144,7 @@ void Context::set_group(uint32_t g) { group_ = std::max<uint32_t>(1, g); }
 
 void Context::set_tuning(const Tuning& t) {
     if (t.crt_tiles != 1 && t.crt_tiles != 2) throw std::invalid_argument("crt_tiles must be 1 or 2");
+    if (t.crt_persistent > 1) throw std::invalid_argument("crt_persistent must be 0 or 1");
     if (t.row_rows > 4096) throw std::invalid_argument("row_rows must be at most 4096");
     tuning_ = t;
     ntt_.row_rows = t.row_rows;
@@ -222,11 +223,19 @@ void Context::negacyclic(uint32_t* pa, uint32_t* pb, size_t plane_stride, uint32
     check(launch_col_inverse(ntt_, pa, plane_stride, count, st), "inverse column pass launch");
 }
 
-void Context::crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint32_t count, cudaStream_t st) {
+void Context::crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint32_t count, cudaStream_t st,
+                  bool tiled) {
     CrtArgs a = crt_;
     a.terms = terms; a.terms_stride = plane_stride;
     a.out = c; a.out_stride = coeff_words();
-    check(launch_crt(a, count, st, tuning_.crt_tiles), "CRT launch");
+    a.terms_tiled = tiled ? 1u : 0u;
+    if (tuning_.crt_persistent || tiled) {
+        // The persistent CRT writes each tile with a bulk copy: 16-byte aligned output.
+        if (reinterpret_cast<uintptr_t>(c) & 15)
+            throw std::invalid_argument("output device pointer must be 16-byte aligned");
+        check(launch_crt_persistent(a, count, st), "CRT launch");
+    }
+    else check(launch_crt(a, count, st, tuning_.crt_tiles), "CRT launch");
 }
 
 void Context::mark_begin(int stage, cudaStream_t st) {
@@ -302,13 +311,15 @@ void Context::chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t 
     begin(kRow);
     check(launch_row_product(ntt_, pa, stride, pb, stride, pa, stride, count, false, st), "row pass launch");
     end();
+    // Tile-major terms for the persistent CRT go to B's planes, dead after the row pass.
+    const bool tiled = tiled_terms();
     if (geom().C > 1) {
         begin(kColInverse);
-        check(launch_col_inverse(ntt_, pa, stride, count, st), "inverse column pass launch");
+        check(launch_col_inverse(ntt_, pa, stride, count, st, tiled ? pb : nullptr), "inverse column pass launch");
         end();
     }
     begin(kCrt);
-    crt(pa, stride, c, count, st);
+    crt(tiled ? pb : pa, stride, c, count, st, tiled);
     end();
 }
 

@@ -108,7 +108,12 @@ public:
     void encode(const uint32_t* a, const uint32_t* b, uint32_t* pa, uint32_t* pb, size_t plane_stride,
                 uint32_t count, cudaStream_t st);
     void negacyclic(uint32_t* pa, uint32_t* pb, size_t plane_stride, uint32_t count, cudaStream_t st);
-    void crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint32_t count, cudaStream_t st);
+    // terms in the natural [P][N] layout, or tile-major ([N/128][P][128], from
+    // launch_col_inverse(..., tiled = true)) when tiled is set.
+    void crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint32_t count, cudaStream_t st,
+             bool tiled = false);
+    // The launch chain hands the CRT tile-major terms when the persistent CRT runs.
+    bool tiled_terms() const { return tuning_.crt_persistent && plan_.g.C > 1 && plan_.g.N >= 128; }
     // Spectral form of an operand: encode + column pass + forward row pass.
     void forward_spectral(const uint32_t* x, uint32_t* planes, cudaStream_t st);
     // c = a * b where a is given in spectral form (planes, shared by all count products).
@@ -183,7 +188,7 @@ private:
 // Autotuner (autotune.cu): times candidate shapes for ctx's geometry, applies
 // the fastest and records it for later Contexts of the same geometry.
 struct AutotuneReport {
-    uint32_t group = 0, crt_tiles = 0, row_rows = 0, row_bits = 0, candidates = 0;
+    uint32_t group = 0, crt_tiles = 0, crt_persistent = 0, row_rows = 0, row_bits = 0, candidates = 0;
     double us_per_product_default = 0, us_per_product_tuned = 0;
 };
 AutotuneReport autotune(Context& ctx, uint32_t max_group);

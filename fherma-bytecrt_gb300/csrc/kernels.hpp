@@ -39,6 +39,7 @@ struct CrtArgs {
     uint32_t* status;
     uint32_t q[kMaxLimbs];
     float invp[256];         // float(1/p_j): warp-uniform reads from the constant cache
+    uint32_t terms_tiled;    // persistent CRT only: terms tile-major, [N/128][P][128]
 };
 
 struct NttArgs;   // ntt.cuh
@@ -47,6 +48,8 @@ struct NttArgs;   // ntt.cuh
 // Kernel shape knobs (the autotuner's search space, bcg_context_set_tuning).
 struct Tuning {
     uint32_t crt_tiles = 2;   // 128-row M tiles per CRT CTA: 2 (shared B chunks) or 1 (two CTAs per SM)
+    uint32_t crt_persistent = 1;   // 1: persistent warp-specialised CRT (crt_tiles unused); measured
+                                   // fastest at N = 16384, 32768 and 65536
     uint32_t row_rows = 0;    // rows of the row pass per CTA; 0: up to 32
 };
 
@@ -57,10 +60,16 @@ size_t crt_smem_bytes(uint32_t NC, uint32_t tiles);
 // Encodes operand A (and operand B when operands == 2) of nprod products (grid.y = operand).
 cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands = 2);
 cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st, uint32_t tiles = 2);
+// Persistent warp-specialised CRT (crt_persistent.cu): same results, overlapped epilogue.
+cudaError_t launch_crt_persistent(const CrtArgs& a, uint32_t nprod, cudaStream_t st);
+size_t crt_persistent_smem_bytes(uint32_t NC, uint32_t L);
 
 // Column passes over nplanes prime-plane sets, set z at planes + z*stride.
 cudaError_t launch_col_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st);
-cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st);
+// tiled_out: write the terms tile-major, [N/128][P][128] per set (N >= 128), into that separate
+// buffer (same stride) for the persistent CRT; null: in place, natural layout.
+cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st,
+                               uint32_t* tiled_out = nullptr);
 cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_t a_stride,
                                const uint32_t* planes_b, size_t b_stride, uint32_t* planes_out,
                                size_t out_stride, uint32_t nprod, bool a_spectral, cudaStream_t st);

@@ -35,9 +35,12 @@ __device__ __forceinline__ void col_exchange(uint32_t (&x)[1 << local_bits(CB)],
     __syncthreads();
 }
 
-template <int CB, bool INVERSE>
+// TILED (inverse only): the terms leave in the CRT's tile-major layout, the
+// 128 coefficients of a tile contiguous per prime, [N/128][P][128], in a
+// separate buffer `out` (a CTA's tile-major positions are other CTAs' inputs).
+template <int CB, bool INVERSE, bool TILED = false>
 __global__ void __launch_bounds__(32 * ((1 << CB) >> local_bits(CB)))
-col_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride) {
+col_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride, uint32_t* __restrict__ out) {
     constexpr int LOCAL = local_bits(CB);
     constexpr int NPH = phase_count(CB);
     const uint32_t R = a.R;                 // column stride: the row length
@@ -68,8 +71,17 @@ col_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride) {
     }
     {
         constexpr PhaseMap<CB, LOCAL> m(last);
+        if constexpr (TILED) {
+            uint32_t* base = out + size_t(blockIdx.z) * plane_stride + (size_t(j) << 7);
 #pragma unroll
-        for (uint32_t k = 0; k < (1u << LOCAL); ++k) col[size_t(m.index(w, k)) * R] = x[k];
+            for (uint32_t k = 0; k < (1u << LOCAL); ++k) {
+                const uint32_t i = blockIdx.x * 32 + lane + m.index(w, k) * R;
+                base[size_t(i >> 7) * (size_t(a.P) << 7) + (i & 127u)] = x[k];
+            }
+        } else {
+#pragma unroll
+            for (uint32_t k = 0; k < (1u << LOCAL); ++k) col[size_t(m.index(w, k)) * R] = x[k];
+        }
     }
 }
 
@@ -260,13 +272,15 @@ row_forward_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride
 }  // namespace
 
 // ---------------------------------------------------------------- launchers --
-template <bool INVERSE>
-static cudaError_t launch_col(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
+template <bool INVERSE, bool TILED = false>
+static cudaError_t launch_col(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st,
+                              uint32_t* out = nullptr) {
     const uint32_t C = a.N / a.R;
     if (C <= 1) return cudaSuccess;
+    if (TILED && (a.N < 128 || a.N % 128 || !out || out == planes)) return cudaErrorInvalidValue;
     const dim3 grid(a.R / 32, a.P, nplanes);
     switch (a.c_bits) {
-#define BCG_COL(CBV) case CBV: col_kernel<CBV, INVERSE><<<grid, 32 * ((1 << CBV) >> local_bits(CBV)), 0, st>>>(a, planes, stride); break;
+#define BCG_COL(CBV) case CBV: col_kernel<CBV, INVERSE, TILED><<<grid, 32 * ((1 << CBV) >> local_bits(CBV)), 0, st>>>(a, planes, stride, out); break;
         BCG_COL(1) BCG_COL(2) BCG_COL(3) BCG_COL(4) BCG_COL(5) BCG_COL(6) BCG_COL(7) BCG_COL(8)
 #undef BCG_COL
         default: return cudaErrorInvalidValue;
@@ -277,8 +291,10 @@ static cudaError_t launch_col(const NttArgs& a, uint32_t* planes, size_t stride,
 cudaError_t launch_col_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
     return launch_col<false>(a, planes, stride, nplanes, st);
 }
-cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
-    return launch_col<true>(a, planes, stride, nplanes, st);
+cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st,
+                               uint32_t* tiled_out) {
+    return tiled_out ? launch_col<true, true>(a, planes, stride, nplanes, st, tiled_out)
+                     : launch_col<true, false>(a, planes, stride, nplanes, st);
 }
 
 static uint32_t row_rows_per_cta(uint32_t C, uint32_t rows_per_iter, uint32_t wanted) {

@@ -76,13 +76,15 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *   "group"      products per launch chain, 1..4096
  *   "crt_tiles"  CRT MMA tile shape: 128-row M tiles per CTA, 2 (each staged
  *                weight-digit chunk feeds both) or 1 (two CTAs per SM)
+ *   "crt_persistent"  1: persistent warp-specialised CRT (one CTA per SM,
+ *                double-buffered accumulators, epilogue overlapping the MMA loop)
  *   "row_rows"   rows per row-pass CTA; 0: up to 32
  *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
  *                Re-plans the twiddle and twist tables (the primes stay). */
 int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value);
 int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* value);
 /* Autotuner: times whole launch chains on synthetic operands for every value
- * of row_bits, then crt_tiles, row_rows and group (coordinate search, at most
+ * of row_bits, then the CRT kernel and tile shape, row_rows and group (coordinate search, at most
  * max_group products per chain and 4 GB of workspace), keeps the fastest, and
  * records it so that contexts of the same geometry created later in the
  * process (including those of bcg_batch and bcg_server) start from it.  The
@@ -90,7 +92,7 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
 typedef struct bcg_autotune_report {
     uint32_t group, crt_tiles, row_rows, row_bits;
     uint32_t candidates;    /* settings timed */
-    uint32_t reserved;
+    uint32_t crt_persistent;
     double us_per_product_default, us_per_product_tuned;
 } bcg_autotune_report;
 int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_report* out);

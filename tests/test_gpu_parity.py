@@ -177,24 +177,26 @@ def test_plugin_abi_roundtrip():
     pkg.fherma_free(st)
 
 
-@pytest.mark.parametrize("N,W", [(64, 100), (2048, 300), (16384, 434), (65536, 1747)])
+@pytest.mark.parametrize("N,W", [(16, 40), (64, 100), (2048, 300), (16384, 434), (32768, 868), (65536, 1747)])
 def test_tuning_knobs_stay_bit_exact(N, W):
-    """Every CRT tile shape and row-pass CTA shape gives the oracle's product."""
+    """Every CRT kernel and tile shape and every row-pass CTA shape gives the oracle's product."""
     pkg = package()
     m, o, q = setup(N, W, 1)
     a = np.stack([pkg.inputs.uniform(q, N, 70 + i) for i in range(3)])
     b = np.stack([pkg.inputs.uniform(q, N, 80 + i) for i in range(3)])
     want = [o.multiply(a[i], b[i]) for i in range(3)]
     da, db = dev(a), dev(b)
-    for tiles in (1, 2):
-        for rows in (0, 8, 64):
-            m.set_tuning("crt_tiles", tiles)
-            m.set_tuning("row_rows", rows)
+    for persistent, tiles, rows in ((0, 1, 0), (0, 2, 8), (0, 1, 64), (1, 2, 0), (1, 2, 64)):
+        m.set_tuning("crt_persistent", persistent)
+        m.set_tuning("crt_tiles", tiles)
+        m.set_tuning("row_rows", rows)
+        for rep in range(2):
             out = torch.zeros_like(da)
             m.multiply_device(da, db, out, 3)
             m.synchronize()
             for i in range(3):
-                assert np.array_equal(host(out[i]), want[i]), (tiles, rows, i)
+                assert np.array_equal(host(out[i]), want[i]), (persistent, tiles, rows, rep, i)
+    m.set_tuning("crt_persistent", 1)
     m.set_tuning("crt_tiles", 2)
     m.set_tuning("row_rows", 0)
 
@@ -233,14 +235,14 @@ def test_autotune_applies_and_is_remembered():
     assert r["candidates"] >= 5
     assert 0 < r["us_per_product_tuned"] <= r["us_per_product_default"] * 1.05
     assert r["crt_tiles"] in (1, 2) and 1 <= r["group"] <= 8
-    for knob in ("group", "crt_tiles", "row_rows", "row_bits"):
+    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_bits"):
         assert m.get_tuning(knob) == r[knob], knob
     a, b = pkg.inputs.uniform(q, N, 3), pkg.inputs.uniform(q, N, 4)
     assert np.array_equal(m.multiply(a, b), O.Oracle(N, W, q).multiply(a, b))
     # Another context of the same geometry (another q) starts from the tuned shapes.
     q2 = pkg.inputs.modulus(W, 32)
     m2 = pkg.Multiplier(N, W, q2)
-    for knob in ("group", "crt_tiles", "row_rows", "row_bits"):
+    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_bits"):
         assert m2.get_tuning(knob) == r[knob], knob
     a2, b2 = pkg.inputs.uniform(q2, N, 5), pkg.inputs.uniform(q2, N, 6)
     assert np.array_equal(m2.multiply(a2, b2), O.Oracle(N, W, q2).multiply(a2, b2))
