@@ -77,6 +77,11 @@ public:
     void synchronize(cudaStream_t st);
     // Stage timing inside the graph: 0 off, k times every k-th chain (recaptures).
     void set_profiling(uint32_t every);
+    // Launch chains alternate over `lanes` parallel branches of the graph (1 or
+    // 2), each with its own workspace, so one chain's kernels can fill the
+    // tail of another's (recaptures).
+    void set_lanes(uint32_t lanes);
+    uint32_t lanes() const { return lanes_; }
     void read_profile(double* ms, uint64_t* launches, uint64_t* timed, uint64_t* chains);
     // Launches per stage and chains of one run (captures the graph if needed).
     void read_counts(uint64_t* launches, uint64_t* chains);
@@ -93,8 +98,10 @@ private:
     PointRegistry reg_;
     std::vector<Group> groups_;
     uint64_t products_ = 0;
-    DeviceBuffer ws_;
-    cudaStream_t capture_stream_ = nullptr;
+    DeviceBuffer ws_, ws2_;
+    cudaStream_t capture_stream_ = nullptr, lane_stream_ = nullptr;
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
+    uint32_t lanes_ = 1;
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     cudaStream_t last_stream_ = nullptr;   // stream of the last graph launch

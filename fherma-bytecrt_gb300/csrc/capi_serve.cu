@@ -69,6 +69,13 @@ int bcg_batch_get_info(bcg_batch* batch, bcg_batch_info* out) {
     });
 }
 
+int bcg_batch_set_lanes(bcg_batch* batch, uint32_t lanes) {
+    return guarded([&] {
+        require(batch, "null batch");
+        batch->batch->set_lanes(lanes);
+    });
+}
+
 int bcg_batch_profile_enable(bcg_batch* batch, int every) {
     return guarded([&] {
         require(batch, "null batch");

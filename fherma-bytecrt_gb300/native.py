@@ -116,6 +116,7 @@ def lib():
         L.bcg_batch_synchronize.argtypes = [vp, vp]
         L.bcg_batch_get_info.argtypes = [vp, ctypes.POINTER(bcg_batch_info)]
         L.bcg_batch_profile_enable.argtypes = [vp, ctypes.c_int]
+        L.bcg_batch_set_lanes.argtypes = [vp, u32]
         L.bcg_batch_profile_read.argtypes = [vp, ctypes.POINTER(bcg_profile)]
         L.bcg_server_create.argtypes = [ctypes.c_int, ctypes.POINTER(bcg_server_options), ctypes.POINTER(vp)]
         L.bcg_server_destroy.argtypes = [vp]
@@ -327,6 +328,10 @@ class Batch:
 
     def profile(self, every: int = 1):
         _check(lib().bcg_batch_profile_enable(self._h, int(every)))
+
+    def set_lanes(self, lanes: int):
+        """Alternate the launch chains over 1 or 2 parallel graph branches."""
+        _check(lib().bcg_batch_set_lanes(self._h, int(lanes)))
 
     def read_profile(self) -> dict:
         p = bcg_profile()

@@ -179,6 +179,9 @@ int bcg_batch_add(bcg_batch* batch, uint32_t N, uint32_t W, uint32_t L, const ui
 int bcg_batch_run(bcg_batch* batch, void* stream);
 int bcg_batch_synchronize(bcg_batch* batch, void* stream);
 int bcg_batch_get_info(bcg_batch* batch, bcg_batch_info* out);   /* captures the graph if needed */
+/* Chains alternate over `lanes` (1 or 2) parallel branches of the graph, each
+ * with its own workspace, so that one chain's kernels fill another's tail. */
+int bcg_batch_set_lanes(bcg_batch* batch, uint32_t lanes);
 /* Stage events inside the graph for every k-th chain (recaptures); the
  * profile holds the stage times of the last completed run. */
 int bcg_batch_profile_enable(bcg_batch* batch, int every);
