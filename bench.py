@@ -259,6 +259,7 @@ def run_native(args):
     # ---- batched B=128, one CUDA graph per step (the headline value).
     batch = pkg.Batch(local)
     batch.add(N, W, q, a_dev, b_dev, c_dev, B)
+    batch.set_lanes(args.lanes)
     batch.profile(every=args.profile_every)
     for _ in range(args.warmup):
         batch.run(stream.cuda_stream)
@@ -353,7 +354,7 @@ def run_native(args):
         "data": "synthetic (seeded uniform operands in [0,q), seeded odd 1747-bit q; 16 distinct products repeated)",
         "config": {"workload": "batched B=128 exact negacyclic products, N=65536 W=1747 L=55 P=114, one q, "
                                "one CUDA graph per step",
-                   "global_batch": B * world, "per_gpu_batch": B, "group": group,
+                   "global_batch": B * world, "per_gpu_batch": B, "group": group, "graph_lanes": args.lanes,
                    "tuning": {k: m.get_tuning(k) for k in ("crt_tiles", "crt_persistent", "row_rows", "row_bits")},
                    "autotune": tuning,
                    "l2": "inputs larger than L2 (3.7 GB per step), no flush", "parallelism": f"replicas x{world}"},
@@ -410,6 +411,7 @@ def run_uneven(pkg, args, stream, device):
             batch.add(n, w, q, ad, bd, cd, count)
             keep.append((ad, bd, cd))
             total_bytes += 3 * ad.numel() * 4
+    batch.set_lanes(args.lanes)
     for _ in range(args.warmup):
         batch.run(stream.cuda_stream)
     torch.cuda.synchronize()
@@ -576,6 +578,9 @@ def main():
                     help="time the stages of every k-th launch chain with CUDA events")
     ap.add_argument("--no-uneven", dest="uneven", action="store_false", help="skip the uneven 96-product batch")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="keep the default kernel shapes")
+    ap.add_argument("--lanes", type=int, default=1, choices=(1, 2),
+                    help="parallel branches of the batch graph that launch chains alternate over (with 2 the "
+                         "stage events of one chain overlap the other chain's kernels, so the roofline reads low)")
     ap.add_argument("--no-served", dest="served", action="store_false", help="skip the served sweep")
     ap.add_argument("--served-loads", default="0.25,0.5,0.75,0.9",
                     help="offered loads as fractions of the estimated capacity")
