@@ -104,6 +104,11 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
             bcg::Tuning t = c.tuning();
             t.crt_tiles = uint32_t(value);
             c.set_tuning(t);
+        } else if (k == "crt_gap_fold") {
+            require(value == 0 || value == 1, "crt_gap_fold must be 0 or 1");
+            bcg::Tuning t = c.tuning();
+            t.crt_gap_fold = uint32_t(value);
+            c.set_tuning(t);
         } else if (k == "crt_persistent") {
             require(value == 0 || value == 1, "crt_persistent must be 0 or 1");
             bcg::Tuning t = c.tuning();
@@ -133,6 +138,8 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         else if (k == "row_rows") *value = c.tuning().row_rows;
         else if (k == "row_bits") *value = c.geom().r_bits;
         else if (k == "crt_persistent") *value = c.tuning().crt_persistent;
+        else if (k == "crt_gap_fold") *value = c.tuning().crt_gap_fold;
+        else if (k == "gap") *value = c.plan().gap;
         else throw std::invalid_argument("unknown tuning knob: " + k);
     });
 }

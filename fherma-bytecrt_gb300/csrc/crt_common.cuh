@@ -30,11 +30,99 @@ __device__ __forceinline__ int64_t limb_value(float f0, float f1, float f2, floa
     return (int64_t(s3) << 24) + (int64_t(s2) << 16) + (int64_t(s1) << 8) + s0;
 }
 
+// q = 2^W - gap with 0 < gap < 2^32 and W > 70 (the form the reference's
+// only reducer handles, native-smoke/g1-crt.cuh:13-68).  Here the CRT sum z
+// is signed (balanced digits times weights in [0, q)), |z| < 2^17 q, so the
+// fold works with the signed high part h = floor(z / 2^W), |h| <= 2^17:
+// z <- (z mod 2^W) + h gap.  A first fold leaves z in [-2^49, 2^W + 2^49);
+// a negative z then has h = -1 and the second fold gives z + q; otherwise z
+// ends below 2q, and z >= q exactly when z + gap >= 2^W, in which case
+// z - q = z + gap - 2^W.  Carries and borrows past the second limb are rare,
+// so each propagation stops as soon as it dies out.
+template <int LT>
+__device__ __forceinline__ void reduce_gap_form(uint32_t* z, int64_t top, const CrtArgs& a, uint32_t L) {
+    const uint32_t r = a.top_bits;                       // 1..32
+    const uint32_t mask = r == 32 ? 0xffffffffu : (1u << r) - 1u;
+    constexpr uint32_t LB = LT ? uint32_t(LT) : 64u;     // compile-time loop bounds keep z in registers
+    int64_t over = top;                                  // signed value of the words above limb L-1
+#pragma unroll
+    for (int fold = 0; fold < 2; ++fold) {
+        const int64_t high = r == 32 ? over : over * (int64_t(1) << (32 - r)) + int64_t(z[L - 1] >> r);
+        z[L - 1] &= mask;
+        const uint64_t m = uint64_t(high < 0 ? -high : high) * a.gap;       // < 2^49: two words
+        const uint32_t w0 = uint32_t(m), w1 = uint32_t(m >> 32);
+        if (high >= 0) {
+            uint64_t s = uint64_t(z[0]) + w0;
+            z[0] = uint32_t(s);
+            s = uint64_t(z[1]) + w1 + (s >> 32);
+            z[1] = uint32_t(s);
+            uint32_t carry = uint32_t(s >> 32);
+#pragma unroll
+            for (uint32_t l = 2; l < LB; ++l) {
+                if (!LT && l >= L) break;
+                if (!carry) break;
+                s = uint64_t(z[l]) + carry;
+                z[l] = uint32_t(s);
+                carry = uint32_t(s >> 32);
+            }
+            over = carry;
+        } else {
+            int64_t s = int64_t(z[0]) - int64_t(w0);
+            z[0] = uint32_t(s);
+            uint32_t borrow = s < 0;
+            s = int64_t(z[1]) - int64_t(w1) - borrow;
+            z[1] = uint32_t(s);
+            borrow = s < 0;
+#pragma unroll
+            for (uint32_t l = 2; l < LB; ++l) {
+                if (!LT && l >= L) break;
+                if (!borrow) break;
+                s = int64_t(z[l]) - 1;
+                z[l] = uint32_t(s);
+                borrow = s < 0;
+            }
+            over = -int64_t(borrow);
+        }
+    }
+    // Now 0 <= z < 2q.  ge: z >= q, either bit W or above is set, or the low W
+    // bits are at least 2^W - gap = [mask][all ones...][2^32 - gap].
+    const int64_t high = r == 32 ? over : over * (int64_t(1) << (32 - r)) + int64_t(z[L - 1] >> r);
+    bool ge = high != 0;
+    if (!ge && (z[L - 1] & mask) == mask && z[0] >= 0u - a.gap) {
+        ge = true;
+#pragma unroll
+        for (uint32_t l = 1; l + 1 < LB; ++l) {
+            if (!LT && l + 1 >= L) break;
+            if (z[l] != 0xffffffffu) { ge = false; break; }
+        }
+    }
+    if (ge) {
+        uint64_t s = uint64_t(z[0]) + a.gap;
+        z[0] = uint32_t(s);
+        uint32_t carry = uint32_t(s >> 32);
+#pragma unroll
+        for (uint32_t l = 1; l < LB; ++l) {
+            if (!LT && l >= L) break;
+            if (!carry) break;
+            s = uint64_t(z[l]) + carry;
+            z[l] = uint32_t(s);
+            carry = uint32_t(s >> 32);
+        }
+        z[L - 1] &= mask;                                 // subtract 2^W
+    }
+}
+
 // Reduces the signed (L+1)-word value (z, top) mod q in place.  k is the
 // floor of the quotient estimated in double precision from the top words
 // (error far below 1), so after z - k q at most one correction remains.
-template <int LT>
+// GAP: -1 decide from a.gap at run time (uniform: a kernel argument), 0 generic
+// only, 1 gap form only (a kernel instantiated per reducer keeps only one).
+template <int LT, int GAP = -1>
 __device__ __forceinline__ void reduce_mod_q(uint32_t* z, int64_t top, const CrtArgs& a, uint32_t L) {
+    if (GAP == 1 || (GAP == -1 && a.gap)) {
+        reduce_gap_form<LT>(z, top, a, L);
+        return;
+    }
     double zhi = double(top);
     const uint32_t T = L < 3 ? L : 3;     // q_inv_scaled = 2^(32(L-T)) / q
 #pragma unroll

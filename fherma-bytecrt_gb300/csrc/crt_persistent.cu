@@ -58,7 +58,7 @@ __device__ __forceinline__ void named_sync(uint32_t id, uint32_t threads) {
     asm volatile("bar.sync %0, %1;" :: "r"(id), "r"(threads) : "memory");
 }
 
-template <int LT>
+template <int LT, int GAP>
 __global__ void __launch_bounds__(kPThreads, 1)
 crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -254,7 +254,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                     top = crt_row_carry<LT>(a, taddr, z);
                     tc_fence_before();
                     mbar_arrive(&ctl->accempty[buf]);          // accumulator read: hand it back
-                    if (valid) reduce_mod_q<LT>(z, top, a, LT);
+                    if (valid) reduce_mod_q<LT, GAP>(z, top, a, LT);
                 }
             }
             // The previous tile's bulk store has read the staging buffer.
@@ -270,7 +270,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                     top = crt_row_carry<0>(a, taddr, zrow);
                     tc_fence_before();
                     mbar_arrive(&ctl->accempty[buf]);
-                    if (valid) reduce_mod_q<0>(zrow, top, a, L);
+                    if (valid) reduce_mod_q<0, GAP>(zrow, top, a, L);
                 }
             }
             fence_proxy_async();
@@ -295,16 +295,22 @@ int sm_count_of_current_device() {
     return sms > 0 ? sms : 1;
 }
 
-template <int LT>
+template <int LT, int GAP>
 cudaError_t launch_persistent_t(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
     const size_t smem = crt_persistent_smem_bytes(a.NC, a.L);
-    cudaError_t e = cudaFuncSetAttribute(crt_persistent_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(crt_persistent_kernel<LT, GAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(smem));
     if (e != cudaSuccess) return e;
     const uint32_t jobs = nprod * ((a.N + kTileRows - 1) / kTileRows);
     const uint32_t grid = std::min<uint32_t>(jobs, uint32_t(sm_count_of_current_device()));
-    crt_persistent_kernel<LT><<<grid, kPThreads, smem, st>>>(a, nprod);
+    crt_persistent_kernel<LT, GAP><<<grid, kPThreads, smem, st>>>(a, nprod);
     return cudaGetLastError();
+}
+
+// One instantiation per reducer: carrying both would raise register pressure.
+template <int LT>
+cudaError_t launch_persistent_l(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
+    return a.gap ? launch_persistent_t<LT, 1>(a, nprod, st) : launch_persistent_t<LT, 0>(a, nprod, st);
 }
 
 }  // namespace
@@ -318,10 +324,10 @@ cudaError_t launch_crt_persistent(const CrtArgs& a, uint32_t nprod, cudaStream_t
     if (reinterpret_cast<uintptr_t>(a.out) & 15) return cudaErrorMisalignedAddress;   // bulk stores
     if (a.terms_tiled && (a.N < kTileRows || a.N % kTileRows)) return cudaErrorInvalidValue;
     switch (a.L) {
-        case 14: return launch_persistent_t<14>(a, nprod, st);
-        case 28: return launch_persistent_t<28>(a, nprod, st);
-        case 55: return launch_persistent_t<55>(a, nprod, st);
-        default: return launch_persistent_t<0>(a, nprod, st);
+        case 14: return launch_persistent_l<14>(a, nprod, st);
+        case 28: return launch_persistent_l<28>(a, nprod, st);
+        case 55: return launch_persistent_l<55>(a, nprod, st);
+        default: return launch_persistent_l<0>(a, nprod, st);
     }
 }
 

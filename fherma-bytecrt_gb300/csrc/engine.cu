@@ -87,6 +87,8 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     crt_.q_inv_scaled = plan_.q_inv_scaled;
     crt_.N = g.N; crt_.L = g.L; crt_.P = g.P; crt_.k_total = g.crt_k_total; crt_.kchunks = g.crt_kchunks;
     crt_.E = g.crt_e; crt_.NC = g.crt_n;
+    crt_.gap = plan_.gap;
+    crt_.top_bits = g.W - 32 * (g.L - 1);
     crt_.status = status_.as<uint32_t>();
 
     // Products per launch chain: long chains amortise each kernel's launch and
@@ -142,12 +144,24 @@ void Context::set_row_bits(uint32_t row_bits) {
 
 void Context::set_group(uint32_t g) { group_ = std::max<uint32_t>(1, g); }
 
+uint32_t Context::host_group() const {
+    // Host-buffer calls pipeline copies against compute in chunks of about
+    // 128 MiB of inputs: the first copy in and the last copy out are not
+    // overlapped, and the host link (~200 GB/s each way) makes them cost
+    // more than the slightly shorter launch chains (4 products per chunk at
+    // N = 65536 measured 5.7% faster end to end than 16).
+    const size_t pair_bytes = 2 * coeff_words() * sizeof(uint32_t);
+    const uint32_t g = uint32_t(std::max<size_t>(1, (size_t(128) << 20) / pair_bytes));
+    return std::min(g, group_);
+}
+
 void Context::set_tuning(const Tuning& t) {
     if (t.crt_tiles != 1 && t.crt_tiles != 2) throw std::invalid_argument("crt_tiles must be 1 or 2");
     if (t.crt_persistent > 1) throw std::invalid_argument("crt_persistent must be 0 or 1");
     if (t.row_rows > 4096) throw std::invalid_argument("row_rows must be at most 4096");
     tuning_ = t;
     ntt_.row_rows = t.row_rows;
+    crt_.gap = t.crt_gap_fold ? plan_.gap : 0u;
 }
 
 void Context::ensure_workspace(uint32_t products) {
@@ -178,7 +192,7 @@ void Context::ensure_host_staging(uint32_t products) {
 // Host buffers that are already pinned: DMA straight from and to them, with
 // two device slots so the copies of one group overlap the compute of the other.
 void Context::multiply_pinned(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count) {
-    const uint32_t g = std::min(group_, count);
+    const uint32_t g = std::min(host_group(), count);
     ensure_workspace(g);
     ensure_device_io(g);
     const size_t cw = coeff_words();
@@ -374,7 +388,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         multiply_pinned(a, b, c, count);
         return;
     }
-    const uint32_t g = std::min(group_, count);
+    const uint32_t g = std::min(host_group(), count);
     ensure_workspace(g);
     ensure_host_staging(g);
     const size_t cw = coeff_words();

@@ -99,6 +99,8 @@ public:
     int device() const { return device_; }
     cudaStream_t stream() const { return stream_; }
     uint32_t group() const { return group_; }
+    // Products per copy/compute chunk of the host-buffer paths.
+    uint32_t host_group() const;
     void set_group(uint32_t g);
     size_t plane_words() const { return size_t(plan_.g.P) * plan_.g.N; }
     size_t coeff_words() const { return size_t(plan_.g.N) * plan_.g.L; }

@@ -40,6 +40,8 @@ struct CrtArgs {
     uint32_t q[kMaxLimbs];
     float invp[256];         // float(1/p_j): warp-uniform reads from the constant cache
     uint32_t terms_tiled;    // persistent CRT only: terms tile-major, [N/128][P][128]
+    uint32_t gap;            // q = 2^W - gap: reduce by two folds (0: generic reduction)
+    uint32_t top_bits;       // W - 32 (L - 1): bits of q's top limb
 };
 
 struct NttArgs;   // ntt.cuh
@@ -51,6 +53,7 @@ struct Tuning {
     uint32_t crt_persistent = 1;   // 1: persistent warp-specialised CRT (crt_tiles unused); measured
                                    // fastest at N = 16384, 32768 and 65536
     uint32_t row_rows = 0;    // rows of the row pass per CTA; 0: up to 32
+    uint32_t crt_gap_fold = 1;   // 1: gap-form q (2^W - gap) reduces by folding; 0: generic reduction
 };
 
 size_t encode_smem_bytes(uint32_t K, uint32_t group_cols);

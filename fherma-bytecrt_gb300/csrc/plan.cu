@@ -401,6 +401,16 @@ HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw, uint3
         }
         plan.q_inv_scaled = double(1.0L / top);
     }
+    {   // Gap form q = 2^W - gap (gap < 2^32): the CRT can reduce by two folds.
+        Big two_w(L, 0);
+        two_w.push_back(0);
+        two_w[(W) / 32] |= 1u << (W % 32);
+        trim(two_w);
+        Big gap = two_w;
+        sub_in_place(gap, q);
+        trim(gap);
+        if (W > 70 && gap.size() == 1) plan.gap = gap[0];
+    }
     return plan;
 }
 

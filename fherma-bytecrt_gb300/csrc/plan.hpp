@@ -41,6 +41,7 @@ struct HostPlan {
     std::vector<uint16_t> crt_b;           // fp16 bit patterns, chunked core-matrix order
     std::vector<float> invp;               // float(1.0 / p_j)
     double q_inv_scaled = 0;               // 2^(32*(L-T)) / q, T = min(L, 3)
+    uint32_t gap = 0;                      // q = 2^W - gap with 0 < gap < 2^32 and W > 70, else 0
     float alpha_error_bound = 0;           // proven bound on |alpha_sum - exact|
 };
 

@@ -78,6 +78,10 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *                weight-digit chunk feeds both) or 1 (two CTAs per SM)
  *   "crt_persistent"  1: persistent warp-specialised CRT (one CTA per SM,
  *                double-buffered accumulators, epilogue overlapping the MMA loop)
+ *   "crt_gap_fold"  1 (default): for q = 2^W - gap (gap < 2^32, W > 70, the
+ *                reference's form) the CRT reduces by two folds instead of the
+ *                generic quotient estimate; 0: always generic
+ *   "gap"        (read only) the gap of a gap-form q, else 0
  *   "row_rows"   rows per row-pass CTA; 0: up to 32
  *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
  *                Re-plans the twiddle and twist tables (the primes stay). */

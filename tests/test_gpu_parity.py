@@ -248,3 +248,39 @@ def test_autotune_applies_and_is_remembered():
     assert np.array_equal(m2.multiply(a2, b2), O.Oracle(N, W, q2).multiply(a2, b2))
     m.close()
     m2.close()
+
+
+@pytest.mark.parametrize("N,W,gap", [(1024, 71, 1), (1024, 96, 5), (2048, 128, (1 << 32) - 1), (4096, 868, 65537),
+                                     (16384, 434, 3), (65536, 1747, 1)])
+def test_gap_form_fold_matches_generic_and_oracle(N, W, gap):
+    """q = 2^W - gap reduces by two folds (the reference's form); the generic
+    reduction gives the same bits, and both equal the oracle, on random and
+    edge operands."""
+    pkg = package()
+    q = pkg.inputs.gap_modulus(W, gap)
+    m = pkg.Multiplier(N, W, q)
+    assert m.get_tuning("gap") == gap
+    o = O.Oracle(N, W, q)
+    cases = [(pkg.inputs.uniform(q, N, 1), pkg.inputs.uniform(q, N, 2)),
+             (pkg.inputs.fixture(q, N, "minus_one"), pkg.inputs.fixture(q, N, "minus_one")),
+             (pkg.inputs.fixture(q, N, "half_high"), pkg.inputs.fixture(q, N, "minus_one")),
+             (pkg.inputs.fixture(q, N, "one"), pkg.inputs.uniform(q, N, 3))]
+    a = np.stack([c[0] for c in cases])
+    b = np.stack([c[1] for c in cases])
+    want = [o.multiply(a[i], b[i]) for i in range(len(cases))]
+    for fold in (1, 0):
+        m.set_tuning("crt_gap_fold", fold)
+        out = torch.zeros((len(cases), N, len(q)), dtype=torch.int32, device="cuda")
+        m.multiply_device(dev(a), dev(b), out, len(cases))
+        m.synchronize()
+        for i in range(len(cases)):
+            assert np.array_equal(host(out[i]), want[i]), (fold, i)
+    m.close()
+
+
+def test_generic_modulus_has_no_gap():
+    pkg = package()
+    q = pkg.inputs.modulus(868, 7)
+    m = pkg.Multiplier(4096, 868, q)
+    assert m.get_tuning("gap") == 0
+    m.close()
