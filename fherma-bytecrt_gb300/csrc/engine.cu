@@ -244,9 +244,9 @@ void Context::crt(const uint32_t* terms, size_t plane_stride, uint32_t* c, uint3
     a.out = c; a.out_stride = coeff_words();
     a.terms_tiled = tiled ? 1u : 0u;
     if (tuning_.crt_persistent || tiled) {
-        // The persistent CRT writes each tile with a bulk copy: 16-byte aligned output.
-        if (reinterpret_cast<uintptr_t>(c) & 15)
-            throw std::invalid_argument("output device pointer must be 16-byte aligned");
+        // The persistent CRT moves terms and output tiles with bulk copies: 16-byte alignment.
+        if ((reinterpret_cast<uintptr_t>(c) | reinterpret_cast<uintptr_t>(terms)) & 15)
+            throw std::invalid_argument("terms and output device pointers must be 16-byte aligned");
         check(launch_crt_persistent(a, count, st), "CRT launch");
     }
     else check(launch_crt(a, count, st, tuning_.crt_tiles), "CRT launch");

@@ -13,7 +13,15 @@
  * BCG_ERR_* code; bcg_last_error() gives a message for the calling thread.
  * Device-pointer entry points take a cudaStream_t passed as void* (NULL means
  * the context's own stream); they are asynchronous.  Host-pointer entry points
- * are synchronous.
+ * are synchronous.  Device buffers must be 16-byte aligned (the kernels move
+ * them with bulk copies).
+ *
+ * Threads: a plan is read-only and may be shared.  A context, a batch and the
+ * stage entry points that use them are not thread-safe: use one per thread,
+ * or serialise calls on it (as the reference's single-threaded harness does,
+ * native-smoke/main.cpp).  Contexts never share mutable state, so different
+ * contexts may run on different threads.  A server is thread-safe: any thread
+ * may submit and wait.
  *
  * The C++ plugin ABI of the reference (fherma_init / fherma_run / fherma_free,
  * native-smoke/fherma.h:46-48, native-batched/fherma.h:47-49) is provided on
@@ -221,7 +229,9 @@ int bcg_server_add_point(bcg_server* server, uint32_t N, uint32_t W, uint32_t L,
 /* Encodes and forward-transforms host operand a ([N][L]) once, synchronously. */
 int bcg_server_add_operand(bcg_server* server, uint32_t point, const uint32_t* a, uint64_t* operand);
 int bcg_server_remove_operand(bcg_server* server, uint64_t operand);
-/* c = a*b; pass a = NULL and operand != 0 to use a resident operand. */
+/* c = a*b; pass a = NULL and operand != 0 to use a resident operand.  The
+ * server keeps each request's result until bcg_server_wait() collects it (or
+ * the server is destroyed): wait for every request you submit. */
 int bcg_server_submit(bcg_server* server, uint32_t point, const uint32_t* a, uint64_t operand,
                       const uint32_t* b, uint32_t* c, uint64_t* request);
 /* Returns the request's own status (BCG_OK or its error), or BCG_ERR_TIMEOUT
