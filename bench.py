@@ -159,6 +159,48 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+def load_tensor_peak():
+    """Sustained dense bf16 TFLOP/s (the kernels are timed inside a long step);
+    fp16 tcgen05 MMAs run at the bf16 rate."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops_sustained"]), "measured (sustained)"
+    except (OSError, ValueError, KeyError):
+        return 1700.0, "fallback (sustained)"
+
+
+def rooflines(info, stage_us, sm_count, sm_mhz):
+    """HBM, tensor and INT32-issue fractions per stage from the live stage times.
+
+    tensor: fp16 digit-MMA FLOPs actually issued (padded K and N) per product;
+    int32 issue: warp instructions per product from the ncu capture of the
+    same kernel (profiles/traffic.json) x 32 lanes, against the SMs' issue
+    peak (4 warp instructions per clock per SM) at the sampled SM clock."""
+    P, L = info.P, info.L
+    hbm_peak, hbm_src = load_peaks()
+    tc_peak, tc_src = load_tensor_peak()
+    alg = algorithmic(info)
+    flops = {"encode": 2.0 * 2 * N * info.enc_k * info.enc_cols, "crt": 2.0 * N * info.crt_k * info.crt_n}
+    insts = load_traffic().get("warp_instructions_per_product", {})
+    issue_peak = sm_count * 4 * 32 * sm_mhz * 1e6          # thread instructions / s
+    out = {"hbm_peak_gbs": hbm_peak, "hbm_peak_source": hbm_src, "tensor_peak_tflops": tc_peak,
+           "tensor_peak_source": tc_src, "issue_peak_tinst_per_s": issue_peak / 1e12, "stages": {}}
+    for s, us in stage_us.items():
+        e = {"us_per_product": us, "hbm_gbs": alg[s] / us / 1e3, "hbm_frac": alg[s] / us / 1e3 / hbm_peak}
+        if s in flops:
+            e["tensor_tflops"] = flops[s] / us / 1e6
+            e["tensor_frac"] = e["tensor_tflops"] / tc_peak
+        if s in insts:
+            e["issue_tinst_per_s"] = insts[s] * 32 / us / 1e6
+            e["issue_frac"] = insts[s] * 32 / (us * 1e-6) / issue_peak
+        out["stages"][s] = e
+    total_us = sum(stage_us.values())
+    out["whole_chain"] = {"us_per_product": total_us, "hbm_gbs": sum(alg.values()) / total_us / 1e3,
+                          "hbm_frac": sum(alg.values()) / total_us / 1e3 / hbm_peak}
+    return out
+
+
 def cpu_baseline(pkg, q, a, b, sample: int):
     from oracle import oracle
     o = oracle.Oracle(N, W, q)
@@ -346,6 +388,10 @@ def run_native(args):
         "stage_ms_per_product": {s: per_launch[s] * launches[s] / B for s in per_launch},
         "timed_launches": prof["timed"][dominant], "profile_every": args.profile_every,
     }
+    clock = clocks.summary()
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    stage_us = {s: 1000 * per_launch[s] * launches[s] / B for s in per_launch}
+    all_rooflines = rooflines(info, stage_us, sm_count, clock["sm_mhz"] or 2070.0)
     cpu = cpu_baseline(pkg, q, a_np, b_np, sample=args.cpu_sample) if args.cpu_sample > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": world, "steps": args.steps,
@@ -368,8 +414,9 @@ def run_native(args):
         "uneven": uneven,
         "served": served,
         "roofline": roofline,
+        "rooflines": all_rooflines,
         "cpu_baseline": cpu,
-        "clocks": clocks.summary(),
+        "clocks": clock,
         "gpu_launches": binfo["launches"] * args.steps,
     }
     print(json.dumps(line), flush=True)
@@ -439,7 +486,7 @@ def run_served(pkg, args, device, batched_value):
     import torch
     rng = np.random.default_rng(77)
     autotune_geometries(pkg, args, device, [(16384, 434), (32768, 868), (65536, 1747)])
-    srv = pkg.Server(device, slots=3)
+    srv = pkg.Server(device, slots=args.served_slots, max_batch=args.served_max_batch)
     mix = [((16384, 434), 0.3, 1), ((32768, 868), 0.4, 2), ((65536, 1747), 0.3, 2)]
     points = []   # (n, w, q, pid, a pool, b pool, resident ids, out ring)
     for (n, w), share, nq in mix:
@@ -586,6 +633,9 @@ def main():
                     help="offered loads as fractions of the estimated capacity")
     ap.add_argument("--served-seconds", type=float, default=1.5, help="arrival window per offered load")
     ap.add_argument("--served-requests", type=int, default=20000, help="cap on requests per offered load")
+    ap.add_argument("--served-slots", type=int, default=3, help="server batches in flight")
+    ap.add_argument("--served-max-batch", type=int, default=0,
+                    help="server products per batch (0: each point's launch-chain length)")
     ap.add_argument("--served-verify", type=int, default=64,
                     help="responses per load compared with the same product run alone")
     args = ap.parse_args()
