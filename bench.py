@@ -43,7 +43,7 @@ sys.path.insert(0, REPO)
 N, W, B = 65536, 1747, 128
 DISTINCT = 16
 METRIC = "exact products/s N=65536 W=1747: batched+served vs plain; p50/p99 latency"
-PUBLISHED_BATCHED = 1427.8   # products/s, reference B=128 whole-call
+PUBLISHED_BATCHED = 1427.8   # products/s: the reference's published B=128 whole-call figure (RTX PRO 6000)
 
 
 def dist_info():
