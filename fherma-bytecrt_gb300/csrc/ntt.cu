@@ -5,11 +5,14 @@
 namespace bcg {
 namespace {
 
-__host__ __device__ constexpr int local_bits(int bits) { return bits < 3 ? bits : 3; }
+// Column pass: 16 elements per thread, 4 levels per phase (C = 256 takes two
+// phases and one exchange; three-level phases took three and two, and
+// measured slower).
+__host__ __device__ constexpr int local_bits(int bits) { return bits < 4 ? bits : 4; }
 
 // ------------------------------------------------------------ column pass --
 // One CTA: 32 adjacent columns (lane = column) of one plane and one prime.
-// Each thread keeps 8 elements of its column in registers per phase of three
+// Each thread keeps 16 elements of its column in registers per phase of four
 // levels; between phases the tile goes through shared memory, one 128-byte
 // row per warp access (conflict free).
 template <int CB, bool INVERSE, int PH>
@@ -42,7 +45,8 @@ template <int CB, bool INVERSE, bool TILED = false>
 __global__ void __launch_bounds__(32 * ((1 << CB) >> local_bits(CB)))
 col_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride, uint32_t* __restrict__ out) {
     constexpr int LOCAL = local_bits(CB);
-    constexpr int NPH = phase_count(CB);
+    constexpr int NPH = phase_count(CB, LOCAL);
+    static_assert(NPH <= 2, "the column pass handles C <= 256 in at most two phases");
     const uint32_t R = a.R;                 // column stride: the row length
     __shared__ uint32_t buf[(1 << CB) * 32];
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;

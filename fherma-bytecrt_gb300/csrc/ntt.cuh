@@ -37,20 +37,22 @@ struct NttArgs {
 };
 
 // Bit positions handled inside one thread during phase `phase` of a transform
-// over `bits` index bits: 3 positions (levels 3*phase .. 3*phase+2 pair bits
-// bits-1-level; short phases are padded with the highest unused positions).
-__host__ __device__ constexpr int phase_count(int bits) { return (bits + 2) / 3; }
+// over `bits` index bits with 2^LOCAL elements per thread: LOCAL positions
+// (levels LOCAL*phase .. LOCAL*phase+LOCAL-1 pair bits bits-1-level; short
+// phases are padded with the highest unused positions).
+__host__ __device__ constexpr int phase_count(int bits, int local = 3) { return (bits + local - 1) / local; }
 
 template <int BITS, int LOCAL>
 struct PhaseMap {
-    int local_pos[3];          // position for k bit 2, 1, 0 (only LOCAL used)
+    int local_pos[4];          // position for k bit LOCAL-1 .. 0 (only LOCAL used, LOCAL <= 4)
     int thread_pos[BITS];      // positions of thread-index bits, ascending
     int levels;                // levels in this phase
     int first_level;
-    __host__ __device__ constexpr PhaseMap(int phase) : local_pos{0, 0, 0}, thread_pos{}, levels(0), first_level(3 * phase) {
+    __host__ __device__ constexpr PhaseMap(int phase)
+        : local_pos{0, 0, 0, 0}, thread_pos{}, levels(0), first_level(LOCAL * phase) {
         bool used[BITS > 0 ? BITS : 1] = {};
         int n = 0;
-        for (int l = first_level; l < first_level + 3 && l < BITS; ++l) {
+        for (int l = first_level; l < first_level + LOCAL && l < BITS; ++l) {
             local_pos[n++] = BITS - 1 - l;
             used[BITS - 1 - l] = true;
         }
