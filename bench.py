@@ -401,7 +401,7 @@ def run_native(args):
         "config": {"workload": "batched B=128 exact negacyclic products, N=65536 W=1747 L=55 P=114, one q, "
                                "one CUDA graph per step",
                    "global_batch": B * world, "per_gpu_batch": B, "group": group, "graph_lanes": args.lanes,
-                   "tuning": {k: m.get_tuning(k) for k in ("crt_tiles", "crt_persistent", "row_rows", "row_bits")},
+                   "tuning": {k: m.get_tuning(k) for k in ("crt_tiles", "crt_persistent", "row_local", "row_rows", "row_bits")},
                    "autotune": tuning,
                    "l2": "inputs larger than L2 (3.7 GB per step), no flush", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": 2 * B * N * L * 4,
@@ -433,7 +433,7 @@ def autotune_geometries(pkg, args, device, geometries):
     for n, w in geometries:
         m = pkg.Multiplier(n, w, pkg.inputs.modulus(w, 1), device=device)
         r = m.autotune(max_group=16)
-        out[f"{n}/{w}"] = {k: r[k] for k in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_bits", "us_per_product_tuned")}
+        out[f"{n}/{w}"] = {k: r[k] for k in ("group", "crt_tiles", "crt_persistent", "row_local", "row_rows", "row_bits", "us_per_product_tuned")}
         m.close()
     return out
 

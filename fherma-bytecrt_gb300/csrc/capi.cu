@@ -104,6 +104,11 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
             bcg::Tuning t = c.tuning();
             t.crt_tiles = uint32_t(value);
             c.set_tuning(t);
+        } else if (k == "row_local") {
+            require(value == 0 || value == 3 || value == 4, "row_local must be 0, 3 or 4");
+            bcg::Tuning t = c.tuning();
+            t.row_local = uint32_t(value);
+            c.set_tuning(t);
         } else if (k == "crt_gap_fold") {
             require(value == 0 || value == 1, "crt_gap_fold must be 0 or 1");
             bcg::Tuning t = c.tuning();
@@ -139,6 +144,7 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         else if (k == "row_bits") *value = c.geom().r_bits;
         else if (k == "crt_persistent") *value = c.tuning().crt_persistent;
         else if (k == "crt_gap_fold") *value = c.tuning().crt_gap_fold;
+        else if (k == "row_local") *value = c.tuning().row_local;
         else if (k == "gap") *value = c.plan().gap;
         else throw std::invalid_argument("unknown tuning knob: " + k);
     });
@@ -152,6 +158,7 @@ int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_repo
         out->group = r.group; out->crt_tiles = r.crt_tiles; out->row_rows = r.row_rows; out->row_bits = r.row_bits;
         out->candidates = r.candidates;
         out->crt_persistent = r.crt_persistent;
+        out->row_local = r.row_local;
         out->us_per_product_default = r.us_per_product_default;
         out->us_per_product_tuned = r.us_per_product_tuned;
     });

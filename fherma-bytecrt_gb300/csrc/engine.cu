@@ -116,7 +116,7 @@ Context::~Context() {
 void Context::bind_ntt() {
     const Geometry& g = plan_.g;
     const TableOffsets off = table_offsets(g);
-    const uint32_t row_rows = ntt_.row_rows;
+    const uint32_t row_rows = ntt_.row_rows, row_local = ntt_.row_local;
     ntt_ = NttArgs{};
     ntt_.consts = geo_->consts.as<uint4>();
     ntt_.tables = geo_->tables.as<uint2>();
@@ -128,6 +128,7 @@ void Context::bind_ntt() {
     ntt_.N = g.N; ntt_.P = g.P; ntt_.c_bits = g.c_bits; ntt_.z_bits = g.z_bits; ntt_.Z = g.Z; ntt_.H = g.H;
     ntt_.R = g.R;
     ntt_.row_rows = row_rows;
+    ntt_.row_local = row_local;
 }
 
 void Context::set_row_bits(uint32_t row_bits) {
@@ -159,8 +160,10 @@ void Context::set_tuning(const Tuning& t) {
     if (t.crt_tiles != 1 && t.crt_tiles != 2) throw std::invalid_argument("crt_tiles must be 1 or 2");
     if (t.crt_persistent > 1) throw std::invalid_argument("crt_persistent must be 0 or 1");
     if (t.row_rows > 4096) throw std::invalid_argument("row_rows must be at most 4096");
+    if (t.row_local != 0 && t.row_local != 3 && t.row_local != 4) throw std::invalid_argument("row_local must be 0, 3 or 4");
     tuning_ = t;
     ntt_.row_rows = t.row_rows;
+    ntt_.row_local = t.row_local;
     crt_.gap = t.crt_gap_fold ? plan_.gap : 0u;
 }
 

@@ -190,7 +190,7 @@ private:
 // Autotuner (autotune.cu): times candidate shapes for ctx's geometry, applies
 // the fastest and records it for later Contexts of the same geometry.
 struct AutotuneReport {
-    uint32_t group = 0, crt_tiles = 0, crt_persistent = 0, row_rows = 0, row_bits = 0, candidates = 0;
+    uint32_t group = 0, crt_tiles = 0, crt_persistent = 0, row_rows = 0, row_local = 0, row_bits = 0, candidates = 0;
     double us_per_product_default = 0, us_per_product_tuned = 0;
 };
 AutotuneReport autotune(Context& ctx, uint32_t max_group);

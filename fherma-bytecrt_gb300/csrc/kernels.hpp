@@ -54,6 +54,7 @@ struct Tuning {
                                    // fastest at N = 16384, 32768 and 65536
     uint32_t row_rows = 0;    // rows of the row pass per CTA; 0: up to 32
     uint32_t crt_gap_fold = 1;   // 1: gap-form q (2^W - gap) reduces by folding; 0: generic reduction
+    uint32_t row_local = 0;      // row pass elements per thread: 0 default, 3 (8 elements) or 4 (16, R = 256)
 };
 
 size_t encode_smem_bytes(uint32_t K, uint32_t group_cols);

@@ -90,54 +90,77 @@ col_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride, uint32
 }
 
 // --------------------------------------------------------------- row pass --
-// TPR = R/8 threads per row, 8 elements each; a warp holds 32/TPR rows.
-// Per row: twist A and B, forward cyclic NTTs, Montgomery pointwise product,
-// inverse cyclic NTT, untwist (with the CRT weight), store into A's plane.
+// TPR = R / 2^RL threads per row, 2^RL elements each; a warp holds 32/TPR
+// rows.  Per row: twist A and B, forward cyclic NTTs, Montgomery pointwise
+// product, inverse cyclic NTT, untwist (with the CRT weight), store into A's
+// plane.  RL = 4 (R = 256: two phases of four levels, one exchange per
+// transform) or RL = 3 (three-level phases, for the shorter rows).
 constexpr int kRowWarps = 8;
 
-template <int RB, int PH>
-__device__ __forceinline__ void row_fwd_phase(uint32_t (&x)[8], uint32_t t, uint32_t p, const uint2* rf) {
-    constexpr PhaseMap<RB, 3> map(PH);
-    phase_ct<RB, 3>(x, map, t, p, [&](int level, uint32_t s) { return rf[(1u << level) + (s >> (RB - level))]; });
+// Row buffer geometry: 16 words of padding per row when RL = 4 put the two
+// rows of a warp on opposite bank halves.
+template <int RB, int RL> struct RowShape {
+    static constexpr uint32_t R = 1u << RB;
+    static constexpr uint32_t TPR = R >> RL;
+    static constexpr uint32_t RPW = 32 / TPR;
+    static constexpr uint32_t kPad = RL == 4 ? 16u : 0u;
+    static constexpr uint32_t kWarpWords = RPW * (R + kPad);   // one operand's rows of a warp
+};
+
+// Shared-memory word of element s inside a row buffer.  RL = 3: swz() keeps
+// the three phase layouts conflict free.  RL = 4: phase 0 writes s = 16k + t
+// and phase 1 reads s = 16t + k; XOR-ing the low nibble with the high one
+// spreads both over distinct banks.
+template <int RL>
+__device__ __forceinline__ uint32_t row_word(uint32_t s) {
+    if constexpr (RL == 4) return s ^ ((s >> 4) & 15u);
+    else return swz(s);
 }
-template <int RB, int PH>
-__device__ __forceinline__ void row_inv_phase(uint32_t (&x)[8], uint32_t t, uint32_t p, const uint2* ri) {
-    constexpr PhaseMap<RB, 3> map(PH);
-    phase_gs<RB, 3>(x, map, t, p, [&](int level, uint32_t s) { return ri[(1u << level) + (s >> (RB - level))]; });
+
+template <int RB, int RL, int PH>
+__device__ __forceinline__ void row_fwd_phase(uint32_t (&x)[1 << RL], uint32_t t, uint32_t p, const uint2* rf) {
+    constexpr PhaseMap<RB, RL> map(PH);
+    phase_ct<RB, RL>(x, map, t, p, [&](int level, uint32_t s) { return rf[(1u << level) + (s >> (RB - level))]; });
 }
-template <int RB, int FROM, int TO>
-__device__ __forceinline__ void row_exchange(uint32_t (&x)[8], uint32_t* rowbuf, uint32_t t) {
-    constexpr PhaseMap<RB, 3> from(FROM), to(TO);
+template <int RB, int RL, int PH>
+__device__ __forceinline__ void row_inv_phase(uint32_t (&x)[1 << RL], uint32_t t, uint32_t p, const uint2* ri) {
+    constexpr PhaseMap<RB, RL> map(PH);
+    phase_gs<RB, RL>(x, map, t, p, [&](int level, uint32_t s) { return ri[(1u << level) + (s >> (RB - level))]; });
+}
+template <int RB, int RL, int FROM, int TO>
+__device__ __forceinline__ void row_exchange(uint32_t (&x)[1 << RL], uint32_t* rowbuf, uint32_t t) {
+    constexpr PhaseMap<RB, RL> from(FROM), to(TO);
 #pragma unroll
-    for (uint32_t k = 0; k < 8; ++k) rowbuf[swz(from.index(t, k))] = x[k];
+    for (uint32_t k = 0; k < (1u << RL); ++k) rowbuf[row_word<RL>(from.index(t, k))] = x[k];
     __syncwarp();
 #pragma unroll
-    for (uint32_t k = 0; k < 8; ++k) x[k] = rowbuf[swz(to.index(t, k))];
+    for (uint32_t k = 0; k < (1u << RL); ++k) x[k] = rowbuf[row_word<RL>(to.index(t, k))];
     __syncwarp();
 }
 
-template <int RB>
-__device__ __forceinline__ void row_forward(uint32_t (&x)[8], uint32_t* rowbuf, uint32_t t, uint32_t p, const uint2* rf) {
-    constexpr int NPH = phase_count(RB);
-    row_fwd_phase<RB, 0>(x, t, p, rf);
-    if constexpr (NPH > 1) { row_exchange<RB, 0, 1>(x, rowbuf, t); row_fwd_phase<RB, 1>(x, t, p, rf); }
-    if constexpr (NPH > 2) { row_exchange<RB, 1, 2>(x, rowbuf, t); row_fwd_phase<RB, 2>(x, t, p, rf); }
+template <int RB, int RL>
+__device__ __forceinline__ void row_forward(uint32_t (&x)[1 << RL], uint32_t* rowbuf, uint32_t t, uint32_t p,
+                                            const uint2* rf) {
+    constexpr int NPH = phase_count(RB, RL);
+    row_fwd_phase<RB, RL, 0>(x, t, p, rf);
+    if constexpr (NPH > 1) { row_exchange<RB, RL, 0, 1>(x, rowbuf, t); row_fwd_phase<RB, RL, 1>(x, t, p, rf); }
+    if constexpr (NPH > 2) { row_exchange<RB, RL, 1, 2>(x, rowbuf, t); row_fwd_phase<RB, RL, 2>(x, t, p, rf); }
 }
-template <int RB>
-__device__ __forceinline__ void row_inverse(uint32_t (&x)[8], uint32_t* rowbuf, uint32_t t, uint32_t p, const uint2* ri) {
-    constexpr int NPH = phase_count(RB);
-    if constexpr (NPH > 2) { row_inv_phase<RB, 2>(x, t, p, ri); row_exchange<RB, 2, 1>(x, rowbuf, t); }
-    if constexpr (NPH > 1) { row_inv_phase<RB, 1>(x, t, p, ri); row_exchange<RB, 1, 0>(x, rowbuf, t); }
-    row_inv_phase<RB, 0>(x, t, p, ri);
+template <int RB, int RL>
+__device__ __forceinline__ void row_inverse(uint32_t (&x)[1 << RL], uint32_t* rowbuf, uint32_t t, uint32_t p,
+                                            const uint2* ri) {
+    constexpr int NPH = phase_count(RB, RL);
+    if constexpr (NPH > 2) { row_inv_phase<RB, RL, 2>(x, t, p, ri); row_exchange<RB, RL, 2, 1>(x, rowbuf, t); }
+    if constexpr (NPH > 1) { row_inv_phase<RB, RL, 1>(x, t, p, ri); row_exchange<RB, RL, 1, 0>(x, rowbuf, t); }
+    row_inv_phase<RB, RL, 0>(x, t, p, ri);
 }
 
-template <int RB>
+template <int RB, int RL>
 __global__ void __launch_bounds__(32 * kRowWarps)
 row_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t* planes_b, size_t b_stride,
            uint32_t* planes_out, size_t out_stride, uint32_t rows_per_cta, uint32_t a_spectral) {
-    constexpr uint32_t R = 1u << RB;
-    constexpr uint32_t TPR = R / 8;
-    constexpr uint32_t RPW = 32 / TPR;
+    using S = RowShape<RB, RL>;
+    constexpr uint32_t R = S::R, TPR = S::TPR, RPW = S::RPW, E = 1u << RL;
     extern __shared__ uint4 smem_raw[];
     uint2* tabs = reinterpret_cast<uint2*>(smem_raw);
     const uint32_t Z = a.Z, H = a.H;
@@ -147,7 +170,7 @@ row_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t*
     uint2* s_tw_hi = s_tw_lo + Z;
     uint2* s_itw_lo = s_tw_hi + H;
     uint2* s_itw_hi = s_itw_lo + Z;
-    uint32_t* xbuf = reinterpret_cast<uint32_t*>(s_itw_hi + H);   // kRowWarps x 2 x 256 words
+    uint32_t* xbuf = reinterpret_cast<uint32_t*>(s_itw_hi + H);   // kRowWarps x 2 x kWarpWords words
 
     const uint32_t j = blockIdx.y;
     const uint4 pc = a.consts[j];
@@ -171,13 +194,13 @@ row_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t*
 
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t t = lane % TPR, rw = lane / TPR;
-    uint32_t* bufa = xbuf + warp * 512 + rw * R;
-    uint32_t* bufb = bufa + 256;
+    uint32_t* bufa = xbuf + warp * 2 * S::kWarpWords + rw * (R + S::kPad);
+    uint32_t* bufb = bufa + S::kWarpWords;
     const uint32_t C = a.N / R;
     const uint32_t zmask = Z - 1;
     const size_t z = blockIdx.z, jn = size_t(j) * a.N;
-    constexpr PhaseMap<RB, 3> m0(0);
-    constexpr PhaseMap<RB, 3> ml(phase_count(RB) - 1);
+    constexpr PhaseMap<RB, RL> m0(0);
+    constexpr PhaseMap<RB, RL> ml(phase_count(RB, RL) - 1);
 
     for (uint32_t it = 0; it * (kRowWarps * RPW) < rows_per_cta; ++it) {
         const uint32_t i2 = blockIdx.x * rows_per_cta + it * (kRowWarps * RPW) + warp * RPW + rw;
@@ -186,32 +209,32 @@ row_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t*
         const uint32_t* rowa = planes_a + z * a_stride + jn + size_t(i2) * R;
         const uint32_t* rowb = planes_b + z * b_stride + jn + size_t(i2) * R;
         uint32_t* rowo = planes_out + z * out_stride + jn + size_t(i2) * R;
-        uint32_t xa[8], xb[8];
+        uint32_t x[E], xb[E];
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) {
-            // A cached in spectral form is stored in the forward transform's output order.
-            xa[k] = valid ? rowa[a_spectral ? ml.index(t, k) : m0.index(t, k)] : 0u;
+        for (uint32_t k = 0; k < E; ++k) {
+            // A cached in spectral form is stored in natural order (element s at s).
+            x[k] = valid ? rowa[a_spectral ? ml.index(t, k) : m0.index(t, k)] : 0u;
             xb[k] = valid ? rowb[m0.index(t, k)] : 0u;
         }
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) {
+        for (uint32_t k = 0; k < E; ++k) {
             const uint32_t e = e0 * m0.index(t, k);
             const uint2 lo = s_tw_lo[e & zmask], hi = s_tw_hi[e >> a.z_bits];
-            if (!a_spectral) xa[k] = mul_shoup(mul_shoup(xa[k], lo.x, lo.y, p), hi.x, hi.y, p);
+            if (!a_spectral) x[k] = mul_shoup(mul_shoup(x[k], lo.x, lo.y, p), hi.x, hi.y, p);
             xb[k] = mul_shoup(mul_shoup(xb[k], lo.x, lo.y, p), hi.x, hi.y, p);
         }
-        if (!a_spectral) row_forward<RB>(xa, bufa, t, p, s_row_f);
-        row_forward<RB>(xb, bufb, t, p, s_row_f);
+        if (!a_spectral) row_forward<RB, RL>(x, bufa, t, p, s_row_f);
+        row_forward<RB, RL>(xb, bufb, t, p, s_row_f);
         // Both operands now sit in the last phase's layout: pointwise product.
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) xa[k] = mul_mont(reduce_once(xa[k], p), xb[k], p, np);
-        row_inverse<RB>(xa, bufa, t, p, s_row_i);
+        for (uint32_t k = 0; k < E; ++k) x[k] = mul_mont(reduce_once(x[k], p), xb[k], p, np);
+        row_inverse<RB, RL>(x, bufa, t, p, s_row_i);
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) {
+        for (uint32_t k = 0; k < E; ++k) {
             const uint32_t s = m0.index(t, k);
             const uint32_t e = e0 * s;
             const uint2 lo = s_itw_lo[e & zmask], hi = s_itw_hi[e >> a.z_bits];
-            uint32_t v = mul_shoup(mul_shoup(xa[k], lo.x, lo.y, p), hi.x, hi.y, p);
+            uint32_t v = mul_shoup(mul_shoup(x[k], lo.x, lo.y, p), hi.x, hi.y, p);
             // With a single row there is no inverse column pass: emit canonical terms here.
             if (C == 1) v = reduce_once(v, p);
             if (valid) rowo[s] = v;
@@ -221,12 +244,11 @@ row_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t*
 
 // Forward row transform only (twist + cyclic NTT), in place: leaves an operand
 // in the spectral form that row_kernel accepts with a_spectral = 1.
-template <int RB>
+template <int RB, int RL>
 __global__ void __launch_bounds__(32 * kRowWarps)
 row_forward_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride, uint32_t rows_per_cta) {
-    constexpr uint32_t R = 1u << RB;
-    constexpr uint32_t TPR = R / 8;
-    constexpr uint32_t RPW = 32 / TPR;
+    using S = RowShape<RB, RL>;
+    constexpr uint32_t R = S::R, TPR = S::TPR, RPW = S::RPW, E = 1u << RL;
     extern __shared__ uint4 smem_raw[];
     uint2* tabs = reinterpret_cast<uint2*>(smem_raw);
     const uint32_t Z = a.Z, H = a.H;
@@ -245,30 +267,30 @@ row_forward_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t t = lane % TPR, rw = lane / TPR;
-    uint32_t* buf = xbuf + warp * 256 + rw * R;
+    uint32_t* buf = xbuf + warp * S::kWarpWords + rw * (R + S::kPad);
     const uint32_t C = a.N / R;
     const uint32_t zmask = Z - 1;
     const size_t plane_off = size_t(blockIdx.z) * plane_stride + size_t(j) * a.N;
-    constexpr PhaseMap<RB, 3> m0(0);
-    constexpr PhaseMap<RB, 3> ml(phase_count(RB) - 1);
+    constexpr PhaseMap<RB, RL> m0(0);
+    constexpr PhaseMap<RB, RL> ml(phase_count(RB, RL) - 1);
     for (uint32_t it = 0; it * (kRowWarps * RPW) < rows_per_cta; ++it) {
         const uint32_t i2 = blockIdx.x * rows_per_cta + it * (kRowWarps * RPW) + warp * RPW + rw;
         const bool valid = i2 < C && it * (kRowWarps * RPW) + warp * RPW + rw < rows_per_cta;
         const uint32_t e0 = 2 * bit_reverse_dev(i2, a.c_bits) + 1;
         uint32_t* row = planes + plane_off + size_t(i2) * R;
-        uint32_t x[8];
+        uint32_t x[E];
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k) {
+        for (uint32_t k = 0; k < E; ++k) {
             const uint32_t s = m0.index(t, k);
             const uint32_t v = valid ? row[s] : 0u;
             const uint32_t e = e0 * s;
             const uint2 lo = s_tw_lo[e & zmask], hi = s_tw_hi[e >> a.z_bits];
             x[k] = mul_shoup(mul_shoup(v, lo.x, lo.y, p), hi.x, hi.y, p);
         }
-        row_forward<RB>(x, buf, t, p, s_row_f);
+        row_forward<RB, RL>(x, buf, t, p, s_row_f);
         // Spectral values are stored in natural (bit-reversed evaluation) order.
 #pragma unroll
-        for (uint32_t k = 0; k < 8; ++k)
+        for (uint32_t k = 0; k < E; ++k)
             if (valid) row[ml.index(t, k)] = x[k];
     }
 }
@@ -301,8 +323,15 @@ cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride
                      : launch_col<true, false>(a, planes, stride, nplanes, st);
 }
 
-static uint32_t row_rows_per_cta(uint32_t C, uint32_t rows_per_iter, uint32_t wanted) {
-    uint32_t rows = wanted ? wanted : 32;
+// Elements per thread of the row pass: 2^3, or 2^4 for R = 256 unless the
+// row_local knob asks for 3.
+static uint32_t row_local_bits(const NttArgs& a) { return (a.R == 256 && a.row_local != 3) ? 4u : 3u; }
+
+// Rows one CTA walks through.  Default 32, or 128 with 16 elements per thread,
+// where a CTA holds 16 rows at a time and the longer walk amortises its table
+// loads (N = 65536: 44.5 against 47.5 us per product).
+static uint32_t row_rows_per_cta(const NttArgs& a, uint32_t C, uint32_t rows_per_iter) {
+    uint32_t rows = a.row_rows ? a.row_rows : (row_local_bits(a) == 4 ? 128 : 32);
     if (rows > C) rows = C;
     if (rows < rows_per_iter) rows = rows_per_iter;
     return rows;
@@ -310,8 +339,11 @@ static uint32_t row_rows_per_cta(uint32_t C, uint32_t rows_per_iter, uint32_t wa
 
 size_t row_smem_bytes(const NttArgs& a, bool forward_only) {
     const uint32_t R = a.R;
+    const uint32_t rl = row_local_bits(a);
+    const uint32_t rpw = 32 / (R >> rl);
+    const size_t warp_words = size_t(rpw) * (R + (rl == 4 ? 16 : 0));
     const size_t tabs = forward_only ? (R + a.Z + a.H) : (2 * R + 2 * a.Z + 2 * a.H);
-    return tabs * sizeof(uint2) + (forward_only ? 1 : 2) * kRowWarps * 256 * sizeof(uint32_t);
+    return tabs * sizeof(uint2) + (forward_only ? 1 : 2) * kRowWarps * warp_words * sizeof(uint32_t);
 }
 
 cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_t a_stride,
@@ -319,16 +351,16 @@ cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_
                                size_t out_stride, uint32_t nprod, bool a_spectral, cudaStream_t st) {
     const uint32_t R = a.R;
     const uint32_t C = a.N / R;
-    const uint32_t rpi = kRowWarps * (32 / (R / 8));
-    const uint32_t rows = row_rows_per_cta(C, rpi, a.row_rows);
+    const uint32_t rpi = kRowWarps * (32 / (R >> row_local_bits(a)));
+    const uint32_t rows = row_rows_per_cta(a, C, rpi);
     const dim3 grid((C + rows - 1) / rows, a.P, nprod);
     const size_t smem = row_smem_bytes(a, false);
-    const uint32_t rb = 31 - __builtin_clz(R);
+    const uint32_t rb = 31 - __builtin_clz(R) + (row_local_bits(a) == 4 ? 8 : 0);   // 16: R = 256, 16 elements
     switch (rb) {
-#define BCG_ROW(RBV) case RBV: \
-        cudaFuncSetAttribute(row_kernel<RBV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
-        row_kernel<RBV><<<grid, 32 * kRowWarps, smem, st>>>(a, planes_a, a_stride, planes_b, b_stride, planes_out, out_stride, rows, a_spectral ? 1u : 0u); break;
-        BCG_ROW(4) BCG_ROW(5) BCG_ROW(6) BCG_ROW(7) BCG_ROW(8)
+#define BCG_ROW(RBV, RLV) case RBV + (RLV == 4 ? 8 : 0): \
+        cudaFuncSetAttribute(row_kernel<RBV, RLV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
+        row_kernel<RBV, RLV><<<grid, 32 * kRowWarps, smem, st>>>(a, planes_a, a_stride, planes_b, b_stride, planes_out, out_stride, rows, a_spectral ? 1u : 0u); break;
+        BCG_ROW(4, 3) BCG_ROW(5, 3) BCG_ROW(6, 3) BCG_ROW(7, 3) BCG_ROW(8, 3) BCG_ROW(8, 4)
 #undef BCG_ROW
         default: return cudaErrorInvalidValue;
     }
@@ -338,16 +370,16 @@ cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_
 cudaError_t launch_row_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st) {
     const uint32_t R = a.R;
     const uint32_t C = a.N / R;
-    const uint32_t rpi = kRowWarps * (32 / (R / 8));
-    const uint32_t rows = row_rows_per_cta(C, rpi, a.row_rows);
+    const uint32_t rpi = kRowWarps * (32 / (R >> row_local_bits(a)));
+    const uint32_t rows = row_rows_per_cta(a, C, rpi);
     const dim3 grid((C + rows - 1) / rows, a.P, nplanes);
     const size_t smem = row_smem_bytes(a, true);
-    const uint32_t rb = 31 - __builtin_clz(R);
+    const uint32_t rb = 31 - __builtin_clz(R) + (row_local_bits(a) == 4 ? 8 : 0);
     switch (rb) {
-#define BCG_ROWF(RBV) case RBV: \
-        cudaFuncSetAttribute(row_forward_kernel<RBV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
-        row_forward_kernel<RBV><<<grid, 32 * kRowWarps, smem, st>>>(a, planes, stride, rows); break;
-        BCG_ROWF(4) BCG_ROWF(5) BCG_ROWF(6) BCG_ROWF(7) BCG_ROWF(8)
+#define BCG_ROWF(RBV, RLV) case RBV + (RLV == 4 ? 8 : 0): \
+        cudaFuncSetAttribute(row_forward_kernel<RBV, RLV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
+        row_forward_kernel<RBV, RLV><<<grid, 32 * kRowWarps, smem, st>>>(a, planes, stride, rows); break;
+        BCG_ROWF(4, 3) BCG_ROWF(5, 3) BCG_ROWF(6, 3) BCG_ROWF(7, 3) BCG_ROWF(8, 3) BCG_ROWF(8, 4)
 #undef BCG_ROWF
         default: return cudaErrorInvalidValue;
     }

@@ -34,6 +34,7 @@ struct NttArgs {
     uint32_t N, P, c_bits, z_bits, Z, H;
     uint32_t R;                // row length of the split N = C * R
     uint32_t row_rows;         // rows of the row pass per CTA (0: up to 32)
+    uint32_t row_local;        // log2 elements per thread in the row pass (0: 4 for R = 256, else 3)
 };
 
 // Bit positions handled inside one thread during phase `phase` of a transform

@@ -46,6 +46,7 @@ class bcg_profile(ctypes.Structure):
 class bcg_autotune_report(ctypes.Structure):
     _fields_ = [("group", ctypes.c_uint32), ("crt_tiles", ctypes.c_uint32), ("row_rows", ctypes.c_uint32),
                 ("row_bits", ctypes.c_uint32), ("candidates", ctypes.c_uint32), ("crt_persistent", ctypes.c_uint32),
+                ("row_local", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
                 ("us_per_product_default", ctypes.c_double), ("us_per_product_tuned", ctypes.c_double)]
 
 
@@ -233,7 +234,7 @@ class Multiplier:
         """Times candidate kernel shapes for this geometry and keeps the fastest."""
         r = bcg_autotune_report()
         _check(lib().bcg_context_autotune(self._h, max_group, ctypes.byref(r)))
-        return {n: getattr(r, n) for n, _ in bcg_autotune_report._fields_}
+        return {n: getattr(r, n) for n, _ in bcg_autotune_report._fields_ if n != "reserved"}
 
     def multiply(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
         a = np.ascontiguousarray(a, dtype=np.uint32)

@@ -90,13 +90,15 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *                reference's form) the CRT reduces by two folds instead of the
  *                generic quotient estimate; 0: always generic
  *   "gap"        (read only) the gap of a gap-form q, else 0
- *   "row_rows"   rows per row-pass CTA; 0: up to 32
+ *   "row_local"  row pass elements per thread: 0 (default: 16 for R = 256, else 8),
+ *                3 (8) or 4 (16, R = 256 only)
+ *   "row_rows"   rows per row-pass CTA; 0: up to 128 with 16 elements per thread, else 32
  *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
  *                Re-plans the twiddle and twist tables (the primes stay). */
 int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value);
 int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* value);
 /* Autotuner: times whole launch chains on synthetic operands for every value
- * of row_bits, then the CRT kernel and tile shape, row_rows and group (coordinate search, at most
+ * of row_bits, then the CRT kernel and tile shape, row_local, row_rows and group (coordinate search, at most
  * max_group products per chain and 4 GB of workspace), keeps the fastest, and
  * records it so that contexts of the same geometry created later in the
  * process (including those of bcg_batch and bcg_server) start from it.  The
@@ -105,6 +107,7 @@ typedef struct bcg_autotune_report {
     uint32_t group, crt_tiles, row_rows, row_bits;
     uint32_t candidates;    /* settings timed */
     uint32_t crt_persistent;
+    uint32_t row_local, reserved;
     double us_per_product_default, us_per_product_tuned;
 } bcg_autotune_report;
 int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_report* out);

@@ -186,10 +186,12 @@ def test_tuning_knobs_stay_bit_exact(N, W):
     b = np.stack([pkg.inputs.uniform(q, N, 80 + i) for i in range(3)])
     want = [o.multiply(a[i], b[i]) for i in range(3)]
     da, db = dev(a), dev(b)
-    for persistent, tiles, rows in ((0, 1, 0), (0, 2, 8), (0, 1, 64), (1, 2, 0), (1, 2, 64)):
+    for persistent, tiles, rows, local in ((0, 1, 0, 3), (0, 2, 8, 0), (0, 1, 64, 3), (1, 2, 0, 0), (1, 2, 64, 0),
+                                           (1, 2, 128, 3)):
         m.set_tuning("crt_persistent", persistent)
         m.set_tuning("crt_tiles", tiles)
         m.set_tuning("row_rows", rows)
+        m.set_tuning("row_local", local)
         for rep in range(2):
             out = torch.zeros_like(da)
             m.multiply_device(da, db, out, 3)
@@ -199,6 +201,7 @@ def test_tuning_knobs_stay_bit_exact(N, W):
     m.set_tuning("crt_persistent", 1)
     m.set_tuning("crt_tiles", 2)
     m.set_tuning("row_rows", 0)
+    m.set_tuning("row_local", 0)
 
 
 @pytest.mark.parametrize("N,W", [(1024, 200), (4096, 868), (32768, 868)])
@@ -235,14 +238,14 @@ def test_autotune_applies_and_is_remembered():
     assert r["candidates"] >= 5
     assert 0 < r["us_per_product_tuned"] <= r["us_per_product_default"] * 1.05
     assert r["crt_tiles"] in (1, 2) and 1 <= r["group"] <= 8
-    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_bits"):
+    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits"):
         assert m.get_tuning(knob) == r[knob], knob
     a, b = pkg.inputs.uniform(q, N, 3), pkg.inputs.uniform(q, N, 4)
     assert np.array_equal(m.multiply(a, b), O.Oracle(N, W, q).multiply(a, b))
     # Another context of the same geometry (another q) starts from the tuned shapes.
     q2 = pkg.inputs.modulus(W, 32)
     m2 = pkg.Multiplier(N, W, q2)
-    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_bits"):
+    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits"):
         assert m2.get_tuning(knob) == r[knob], knob
     a2, b2 = pkg.inputs.uniform(q2, N, 5), pkg.inputs.uniform(q2, N, 6)
     assert np.array_equal(m2.multiply(a2, b2), O.Oracle(N, W, q2).multiply(a2, b2))
