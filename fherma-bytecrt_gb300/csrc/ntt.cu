@@ -117,15 +117,47 @@ __device__ __forceinline__ uint32_t row_word(uint32_t s) {
     else return swz(s);
 }
 
+// Row twiddle tables in shared memory.  Level l uses entries 2^l + u,
+// u = s >> (RB - l).  With R = 256 and 16 elements per thread, phase 1
+// (levels 4-7) holds s = 16t + k, so u = t * 2^(l-4) + c with c from k: in
+// natural order the 16 threads of a row would read entries 2^(l-4) apart
+// (up to 8-way bank conflicts on the 8-byte entries).  Those levels are
+// stored c-major instead, entry 2^l + c*16 + t, so the threads of a row read
+// 16 consecutive entries.  Phase 0 reads one entry per level for all threads
+// (a broadcast) and keeps the natural order.
+template <int RB, int RL>
+__host__ __device__ constexpr bool row_tw_cmajor() { return RB == 8 && RL == 4; }
+
+// Position of natural entry i (1 <= i < R) in the shared-memory table.
+template <int RB, int RL>
+__device__ __forceinline__ uint32_t row_tw_slot(uint32_t i) {
+    if constexpr (row_tw_cmajor<RB, RL>()) {
+        if (i < 16) return i;
+        const uint32_t l = 31u - __clz(i), u = i - (1u << l);
+        return (1u << l) + ((u & ((1u << (l - 4)) - 1u)) << 4) + (u >> (l - 4));
+    } else {
+        return i;
+    }
+}
+
+template <int RB, int RL>
+__device__ __forceinline__ uint2 row_twiddle(const uint2* tab, int level, uint32_t s) {
+    const uint32_t u = s >> (RB - level);
+    if constexpr (row_tw_cmajor<RB, RL>()) {
+        if (level >= 4) return tab[(1u << level) + ((u & ((1u << (level - 4)) - 1u)) << 4) + (s >> 4)];
+    }
+    return tab[(1u << level) + u];
+}
+
 template <int RB, int RL, int PH>
 __device__ __forceinline__ void row_fwd_phase(uint32_t (&x)[1 << RL], uint32_t t, uint32_t p, const uint2* rf) {
     constexpr PhaseMap<RB, RL> map(PH);
-    phase_ct<RB, RL>(x, map, t, p, [&](int level, uint32_t s) { return rf[(1u << level) + (s >> (RB - level))]; });
+    phase_ct<RB, RL>(x, map, t, p, [&](int level, uint32_t s) { return row_twiddle<RB, RL>(rf, level, s); });
 }
 template <int RB, int RL, int PH>
 __device__ __forceinline__ void row_inv_phase(uint32_t (&x)[1 << RL], uint32_t t, uint32_t p, const uint2* ri) {
     constexpr PhaseMap<RB, RL> map(PH);
-    phase_gs<RB, RL>(x, map, t, p, [&](int level, uint32_t s) { return ri[(1u << level) + (s >> (RB - level))]; });
+    phase_gs<RB, RL>(x, map, t, p, [&](int level, uint32_t s) { return row_twiddle<RB, RL>(ri, level, s); });
 }
 template <int RB, int RL, int FROM, int TO>
 __device__ __forceinline__ void row_exchange(uint32_t (&x)[1 << RL], uint32_t* rowbuf, uint32_t t) {
@@ -178,8 +210,9 @@ row_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t*
     {
         const uint2* g = a.tables + size_t(j) * a.table_stride;
         for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) {
-            s_row_f[i] = g[a.off_row_f + i];
-            s_row_i[i] = g[a.off_row_i + i];
+            const uint32_t slot = i ? row_tw_slot<RB, RL>(i) : 0u;
+            s_row_f[slot] = g[a.off_row_f + i];
+            s_row_i[slot] = g[a.off_row_i + i];
         }
         for (uint32_t i = threadIdx.x; i < Z; i += blockDim.x) {
             s_tw_lo[i] = g[a.off_tw_lo + i];
@@ -260,7 +293,7 @@ row_forward_kernel(NttArgs a, uint32_t* __restrict__ planes, size_t plane_stride
     const uint32_t p = a.consts[j].x;
     {
         const uint2* g = a.tables + size_t(j) * a.table_stride;
-        for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_row_f[i] = g[a.off_row_f + i];
+        for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) s_row_f[i ? row_tw_slot<RB, RL>(i) : 0u] = g[a.off_row_f + i];
         for (uint32_t i = threadIdx.x; i < Z; i += blockDim.x) s_tw_lo[i] = g[a.off_tw_lo + i];
         for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) s_tw_hi[i] = g[a.off_tw_hi + i];
     }
