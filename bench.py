@@ -244,7 +244,23 @@ def run_reference(args):
                          "sample": f"{per_step} product per step, {args.steps} steps"},
         "e2e": {"value": value, "unit": "products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    line["gpu_kernels"] = reference_gpu_kernels()
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_kernels():
+    """The reference's own encode_mma32 and g1_crt32 kernels (compiled unmodified from its
+    sources into oracle/_ref/ref_kernels.cubin), checked against the oracle and timed on this
+    GPU, one product per launch as the reference launches them; None where the cubin or a GPU
+    is missing."""
+    try:
+        import torch
+        from oracle import ref_kernels
+        if not (ref_kernels.available() and torch.cuda.is_available()):
+            return None
+        return [ref_kernels.run(n, w) for n, w in ((65536, 1747), (32768, 868))]
+    except Exception as e:          # reported, never fatal for the CPU arm
+        return {"error": str(e)[:200]}
 
 
 def run_native(args):

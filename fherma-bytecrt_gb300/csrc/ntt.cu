@@ -360,11 +360,28 @@ cudaError_t launch_col_inverse(const NttArgs& a, uint32_t* planes, size_t stride
 // row_local knob asks for 3.
 static uint32_t row_local_bits(const NttArgs& a) { return (a.R == 256 && a.row_local != 3) ? 4u : 3u; }
 
+static uint32_t sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return uint32_t(n);
+}
+
 // Rows one CTA walks through.  Default 32, or 128 with 16 elements per thread,
 // where a CTA holds 16 rows at a time and the longer walk amortises its table
-// loads (N = 65536: 44.5 against 47.5 us per product).
-static uint32_t row_rows_per_cta(const NttArgs& a, uint32_t C, uint32_t rows_per_iter) {
+// loads (N = 65536, 16 products: 44.5 against 47.5 us per product).  A default
+// is halved while the grid would give fewer than four CTAs per SM (one
+// product per launch: N = 32768 has only 57 rows of CTAs at 128 rows each).
+static uint32_t row_rows_per_cta(const NttArgs& a, uint32_t C, uint32_t rows_per_iter, uint32_t nprod) {
     uint32_t rows = a.row_rows ? a.row_rows : (row_local_bits(a) == 4 ? 128 : 32);
+    if (!a.row_rows) {
+        const uint64_t want = 4ull * sm_count();
+        while (rows > rows_per_iter && uint64_t((C + rows - 1) / rows) * a.P * nprod < want) rows /= 2;
+    }
     if (rows > C) rows = C;
     if (rows < rows_per_iter) rows = rows_per_iter;
     return rows;
@@ -385,7 +402,7 @@ cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_
     const uint32_t R = a.R;
     const uint32_t C = a.N / R;
     const uint32_t rpi = kRowWarps * (32 / (R >> row_local_bits(a)));
-    const uint32_t rows = row_rows_per_cta(a, C, rpi);
+    const uint32_t rows = row_rows_per_cta(a, C, rpi, nprod);
     const dim3 grid((C + rows - 1) / rows, a.P, nprod);
     const size_t smem = row_smem_bytes(a, false);
     const uint32_t rb = 31 - __builtin_clz(R) + (row_local_bits(a) == 4 ? 8 : 0);   // 16: R = 256, 16 elements
@@ -404,7 +421,7 @@ cudaError_t launch_row_forward(const NttArgs& a, uint32_t* planes, size_t stride
     const uint32_t R = a.R;
     const uint32_t C = a.N / R;
     const uint32_t rpi = kRowWarps * (32 / (R >> row_local_bits(a)));
-    const uint32_t rows = row_rows_per_cta(a, C, rpi);
+    const uint32_t rows = row_rows_per_cta(a, C, rpi, nplanes);
     const dim3 grid((C + rows - 1) / rows, a.P, nplanes);
     const size_t smem = row_smem_bytes(a, true);
     const uint32_t rb = 31 - __builtin_clz(R) + (row_local_bits(a) == 4 ? 8 : 0);
