@@ -69,6 +69,19 @@ __device__ __forceinline__ void bfly_gs(uint32_t& x, uint32_t& y, uint2 w, uint3
     y = mul_shoup(xr - yr + p, w.x, w.y, p);
 }
 
+// The same butterflies for a twiddle of 1: no multiply.
+__device__ __forceinline__ void bfly_ct_unit(uint32_t& x, uint32_t& y, uint32_t p) {
+    const uint32_t t = reduce_once(y, p);
+    const uint32_t xr = reduce_once(x, p);
+    x = xr + t;
+    y = xr - t + p;
+}
+__device__ __forceinline__ void bfly_gs_unit(uint32_t& x, uint32_t& y, uint32_t p) {
+    const uint32_t xr = reduce_once(x, p), yr = reduce_once(y, p);
+    x = xr + yr;
+    y = xr - yr + p;
+}
+
 // ---------------------------------------------------- fp16 byte digits -----
 // Balanced base-256 digits in [-128, 128] are exact in fp16.  0x64XX is the
 // fp16 bit pattern of 1024 + XX, so a byte b becomes fp16(b - bias) with one

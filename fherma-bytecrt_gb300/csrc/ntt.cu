@@ -152,12 +152,12 @@ __device__ __forceinline__ uint2 row_twiddle(const uint2* tab, int level, uint32
 template <int RB, int RL, int PH>
 __device__ __forceinline__ void row_fwd_phase(uint32_t (&x)[1 << RL], uint32_t t, uint32_t p, const uint2* rf) {
     constexpr PhaseMap<RB, RL> map(PH);
-    phase_ct<RB, RL>(x, map, t, p, [&](int level, uint32_t s) { return row_twiddle<RB, RL>(rf, level, s); });
+    phase_ct<RB, RL, true>(x, map, t, p, [&](int level, uint32_t s) { return row_twiddle<RB, RL>(rf, level, s); });
 }
 template <int RB, int RL, int PH>
 __device__ __forceinline__ void row_inv_phase(uint32_t (&x)[1 << RL], uint32_t t, uint32_t p, const uint2* ri) {
     constexpr PhaseMap<RB, RL> map(PH);
-    phase_gs<RB, RL>(x, map, t, p, [&](int level, uint32_t s) { return row_twiddle<RB, RL>(ri, level, s); });
+    phase_gs<RB, RL, true>(x, map, t, p, [&](int level, uint32_t s) { return row_twiddle<RB, RL>(ri, level, s); });
 }
 template <int RB, int RL, int FROM, int TO>
 __device__ __forceinline__ void row_exchange(uint32_t (&x)[1 << RL], uint32_t* rowbuf, uint32_t t) {

@@ -80,8 +80,16 @@ __device__ __forceinline__ uint32_t swz(uint32_t s) {
     return s ^ ((h << 2) | (h & 3u));
 }
 
+// In the first phase the block index of level l is k >> (LOCAL - l), known at
+// compile time.  UNIT0: the transform's block-0 twiddles are 1 (the cyclic row
+// transforms), so those butterflies skip the multiply.
+template <int LOCAL>
+__device__ __forceinline__ constexpr bool unit_block(int first_level, int li, uint32_t k) {
+    return first_level == 0 && (k >> (LOCAL - li)) == 0;
+}
+
 // Forward CT levels of one phase on a thread's LOCAL elements; `twiddle(level, s)`.
-template <int BITS, int LOCAL, class Tw>
+template <int BITS, int LOCAL, bool UNIT0 = false, class Tw>
 __device__ __forceinline__ void phase_ct(uint32_t (&x)[1 << LOCAL], const PhaseMap<BITS, LOCAL>& map,
                                          uint32_t t, uint32_t p, Tw twiddle) {
 #pragma unroll
@@ -91,6 +99,7 @@ __device__ __forceinline__ void phase_ct(uint32_t (&x)[1 << LOCAL], const PhaseM
 #pragma unroll
         for (uint32_t k = 0; k < (1u << LOCAL); ++k) {
             if (k & bit) continue;
+            if (UNIT0 && unit_block<LOCAL>(map.first_level, li, k)) { bfly_ct_unit(x[k], x[k | bit], p); continue; }
             const uint32_t s = map.index(t, k);
             const uint2 w = twiddle(level, s);
             bfly_ct(x[k], x[k | bit], w, p);
@@ -98,7 +107,7 @@ __device__ __forceinline__ void phase_ct(uint32_t (&x)[1 << LOCAL], const PhaseM
     }
 }
 
-template <int BITS, int LOCAL, class Tw>
+template <int BITS, int LOCAL, bool UNIT0 = false, class Tw>
 __device__ __forceinline__ void phase_gs(uint32_t (&x)[1 << LOCAL], const PhaseMap<BITS, LOCAL>& map,
                                          uint32_t t, uint32_t p, Tw twiddle) {
 #pragma unroll
@@ -108,6 +117,7 @@ __device__ __forceinline__ void phase_gs(uint32_t (&x)[1 << LOCAL], const PhaseM
 #pragma unroll
         for (uint32_t k = 0; k < (1u << LOCAL); ++k) {
             if (k & bit) continue;
+            if (UNIT0 && unit_block<LOCAL>(map.first_level, li, k)) { bfly_gs_unit(x[k], x[k | bit], p); continue; }
             const uint32_t s = map.index(t, k);
             const uint2 w = twiddle(level, s);
             bfly_gs(x[k], x[k | bit], w, p);
