@@ -76,7 +76,8 @@ def build(verbose: bool = False) -> str:
         shim = os.path.join(HERE, f"libfherma_gb300{suffix}.so")
         if _stale(shim, [shim_src, LIB, *_headers()]):
             tmp = shim + f".tmp{os.getpid()}"
-            subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", *defs, *inc, "-o", tmp, shim_src,
+            subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-Wl,--wrap=memcpy",
+                            "-Wl,--wrap=memmove", *defs, *inc, "-o", tmp, shim_src,
                             "-L", HERE, "-lbytecrt_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
             os.replace(tmp, shim)
         harness = os.path.join(HERE, f"solution{suffix}")

@@ -164,6 +164,16 @@ int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_repo
     });
 }
 
+int bcg_multiply_sink(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t count, bcg_sink sink,
+                      void* user) {
+    return guarded([&] {
+        require(ctx && sink, "null argument");
+        if (count == 0) return;
+        require(a && b, "null buffer");
+        ctx->ctx->multiply_host(a, b, nullptr, count, sink, user);
+    });
+}
+
 int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count) {
     return guarded([&] {
         require(ctx, "null context");

@@ -72,6 +72,12 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     upload(q_, plan_.q.data(), plan_.q.size() * 4);
     status_.allocate(16);
     check(cudaMemset(status_.ptr, 0, 16), "status reset");
+    {
+        int pageable = 0, host_tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device_);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device_);
+        pageable_direct_ = pageable && host_tables;
+    }
 
     bind_ntt();
 
@@ -107,6 +113,7 @@ Context::~Context() {
         if (ev_in_[s]) cudaEventDestroy(ev_in_[s]);
         if (ev_done_[s]) cudaEventDestroy(ev_done_[s]);
         if (ev_out_[s]) cudaEventDestroy(ev_out_[s]);
+        for (cudaEvent_t e : piece_ev_[s]) cudaEventDestroy(e);
     }
     if (copy_in_) cudaStreamDestroy(copy_in_);
     if (copy_out_) cudaStreamDestroy(copy_out_);
@@ -385,9 +392,10 @@ bool is_pinned(const void* p) {
 }
 }  // namespace
 
-void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count) {
+void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, Sink sink,
+                            void* user) {
     if (count == 0) return;
-    if (is_pinned(a) && is_pinned(b) && is_pinned(c)) {
+    if (!sink && is_pinned(a) && is_pinned(b) && is_pinned(c)) {
         multiply_pinned(a, b, c, count);
         return;
     }
@@ -397,11 +405,38 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     const size_t cw = coeff_words();
     const uint32_t ngroups = (count + g - 1) / g;
     auto group_size = [&](uint32_t gi) { return std::min(g, count - gi * g); };
+    // Staged copies move in pieces: the host packs piece k+1 (or unpacks
+    // piece k-1) while the DMA engine moves piece k.
+    constexpr size_t kPiece = size_t(4) << 20;
+    const size_t max_pieces = (size_t(g) * cw * 4 + kPiece - 1) / kPiece;
+    for (int s = 0; s < 2; ++s)
+        while (piece_ev_[s].size() < max_pieces) {
+            cudaEvent_t e;
+            check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            piece_ev_[s].push_back(e);
+        }
     auto drain = [&](uint32_t gi) {
         const int s = gi & 1;
-        check(cudaEventSynchronize(ev_out_[s]), "output copy");
-        const size_t words = size_t(group_size(gi)) * cw;
-        parallel_copy(c + size_t(gi) * g * cw, io_host_[s].as<uint32_t>() + 2 * g * cw, words * 4);
+        const size_t bytes = size_t(group_size(gi)) * cw * 4;
+        const char* src = reinterpret_cast<const char*>(io_host_[s].as<uint32_t>() + 2 * g * cw);
+        char* dst = reinterpret_cast<char*>(c + size_t(gi) * g * cw);
+        for (size_t k = 0, off = 0; off < bytes; ++k, off += kPiece) {
+            const size_t n = std::min(kPiece, bytes - off);
+            check(cudaEventSynchronize(piece_ev_[s][k]), "output copy");
+            if (sink) sink(user, reinterpret_cast<const uint32_t*>(src + off), n / 4);
+            else parallel_copy(dst + off, src + off, n);
+        }
+    };
+    auto stage_in = [&](char* h, char* d, const char* x, size_t bytes) {
+        if (pageable_direct_) {   // the DMA engine reads the caller's buffer itself
+            check(cudaMemcpyAsync(d, x, bytes, cudaMemcpyHostToDevice, copy_in_), "input copy");
+            return;
+        }
+        for (size_t off = 0; off < bytes; off += kPiece) {
+            const size_t n = std::min(kPiece, bytes - off);
+            parallel_copy(h + off, x + off, n);
+            check(cudaMemcpyAsync(d + off, h + off, n, cudaMemcpyHostToDevice, copy_in_), "input copy");
+        }
     };
     for (uint32_t gi = 0; gi < ngroups; ++gi) {
         const int s = gi & 1;
@@ -410,19 +445,24 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         const size_t words = size_t(n) * cw;
         uint32_t* h = io_host_[s].as<uint32_t>();
         uint32_t* d = io_dev_[s].as<uint32_t>();
-        parallel_copy(h, a + size_t(gi) * g * cw, words * 4);
-        parallel_copy(h + g * cw, b + size_t(gi) * g * cw, words * 4);
         if (gi >= 2) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
-        check(cudaMemcpyAsync(d, h, words * 4, cudaMemcpyHostToDevice, copy_in_), "input copy");
-        check(cudaMemcpyAsync(d + g * cw, h + g * cw, words * 4, cudaMemcpyHostToDevice, copy_in_), "input copy");
+        stage_in(reinterpret_cast<char*>(h), reinterpret_cast<char*>(d),
+                 reinterpret_cast<const char*>(a + size_t(gi) * g * cw), words * 4);
+        stage_in(reinterpret_cast<char*>(h + g * cw), reinterpret_cast<char*>(d + g * cw),
+                 reinterpret_cast<const char*>(b + size_t(gi) * g * cw), words * 4);
         check(cudaEventRecord(ev_in_[s], copy_in_), "event");
         check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
         chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_);
         check(cudaEventRecord(ev_done_[s], stream_), "event");
         check(cudaStreamWaitEvent(copy_out_, ev_done_[s], 0), "event wait");
-        check(cudaMemcpyAsync(h + 2 * g * cw, d + 2 * g * cw, words * 4, cudaMemcpyDeviceToHost, copy_out_),
-              "output copy");
-        check(cudaEventRecord(ev_out_[s], copy_out_), "event");
+        const size_t bytes = words * 4;
+        for (size_t k = 0, off = 0; off < bytes; ++k, off += kPiece) {
+            const size_t pn = std::min(kPiece, bytes - off);
+            check(cudaMemcpyAsync(reinterpret_cast<char*>(h + 2 * g * cw) + off,
+                                  reinterpret_cast<const char*>(d + 2 * g * cw) + off, pn,
+                                  cudaMemcpyDeviceToHost, copy_out_), "output copy");
+            check(cudaEventRecord(piece_ev_[s][k], copy_out_), "event");
+        }
     }
     for (uint32_t gi = ngroups >= 2 ? ngroups - 2 : 0; gi < ngroups; ++gi) drain(gi);
     check_status();

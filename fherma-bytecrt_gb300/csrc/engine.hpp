@@ -124,7 +124,11 @@ public:
 
     // Whole products.
     void multiply_device(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, cudaStream_t st);
-    void multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
+    // Host buffers.  With a sink, c is unused: the product goes to
+    // sink(user, words, n) in order, one staged piece at a time.
+    using Sink = void (*)(void* user, const uint32_t* words, size_t n);
+    void multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count,
+                       Sink sink = nullptr, void* user = nullptr);
 
     // Throws DeviceTimeout (after clearing it) if a kernel reported a wait timeout.
     void synchronize(cudaStream_t st);
@@ -169,6 +173,9 @@ private:
 
     HostPlan plan_;
     int device_ = 0;
+    // The copy engines read pageable host memory through the host page tables
+    // (coherent CPU-GPU systems): host inputs then skip the pinned staging copy.
+    bool pageable_direct_ = false;
     cudaStream_t stream_ = nullptr;
     cudaStream_t copy_in_ = nullptr, copy_out_ = nullptr;
     uint32_t group_ = 1;
@@ -181,6 +188,7 @@ private:
     PinnedBuffer io_host_[2];
     size_t io_products_ = 0, io_dev_products_ = 0;
     cudaEvent_t ev_in_[2] = {}, ev_done_[2] = {}, ev_out_[2] = {};
+    std::vector<cudaEvent_t> piece_ev_[2];   // staged output pieces of each slot
     NttArgs ntt_{};
     EncodeArgs enc_{};
     CrtArgs crt_{};

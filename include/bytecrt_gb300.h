@@ -116,6 +116,15 @@ int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_repo
  * bcg_multiply: host buffers, synchronous; replaces fherma_run
  * (native-smoke/solve.cu:506-525; batched native-batched/solve.cu:200-244). */
 int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
+/* Like bcg_multiply, but the product ([count][N][L] words) is handed over in
+ * order, in consecutive runs, to sink(user, words, n) as each run arrives on
+ * the host; `words` is valid only during the call, and the sink must not
+ * throw.  For callers that build their own output container (the plugin's
+ * owned std::vector) without filling it first.  No counterpart in the
+ * reference. */
+typedef void (*bcg_sink)(void* user, const uint32_t* words, size_t n);
+int bcg_multiply_sink(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t count, bcg_sink sink,
+                      void* user);
 /* device buffers, asynchronous on `stream` */
 int bcg_multiply_device(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c,
                         uint32_t count, void* stream);
