@@ -429,6 +429,7 @@ def run_native(args):
                   "batched_over_plain_e2e": e2e_value / world / (1000.0 / plain_e2e_ms)},
         "uneven": uneven,
         "served": served,
+        "plugin": run_plugin(pkg, args) if (args.plugin and rank == 0) else None,
         "roofline": roofline,
         "rooflines": all_rooflines,
         "cpu_baseline": cpu,
@@ -439,6 +440,56 @@ def run_native(args):
     batch.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_plugin(pkg, args):
+    """The drop-in path as the challenge harness drives it: the `solution` and
+    `solution_batched` binaries (the reference's wire format and per-case timer
+    around fherma_run, with caller-owned pageable std::vector operands and an
+    owned output vector) on N=65536/W=1747 cases.  Milliseconds per product,
+    median over the cases after the first."""
+    import shutil
+    import subprocess
+    import tempfile
+    import numpy as np
+    pkg_dir = os.path.dirname(os.path.abspath(pkg.__file__))
+    q = pkg.inputs.gap_modulus(W, 0x9E3779B1)
+    L = len(q)
+    out = {"point": f"N={N} W={W} q=2^{W}-2654435761, pageable host vectors"}
+    for name, B, cases in (("solution", 1, 6), ("solution_batched", 16, 4)):
+        exe = os.path.join(pkg_dir, name)
+        if not os.path.exists(exe):
+            out[name] = None
+            continue
+        root = tempfile.mkdtemp(prefix="bcg_plugin_")
+        try:
+            man = {"N": N, "W": W, "L": L, "cases": cases}
+            if name.endswith("batched"):
+                man["B"] = B
+            os.makedirs(os.path.join(root, "point"))
+            with open(os.path.join(root, "manifest.json"), "w") as f:
+                json.dump(man, f)
+            q.astype("<u4").tofile(os.path.join(root, "point", "q.bin"))
+            for i in range(cases):
+                d = os.path.join(root, "cases", f"{i:06d}")
+                os.makedirs(d)
+                for k, tag in ((0, "a"), (1, "b")):
+                    x = np.stack([pkg.inputs.uniform(q, N, 7000 + 100 * i + 2 * j + k) for j in range(B)])
+                    x.astype("<u4").tofile(os.path.join(d, f"{tag}.bin"))
+            r = subprocess.run([exe, root], capture_output=True, text=True, timeout=600)
+            res = json.load(open(os.path.join(root, "out", "results.json")))
+            ms = [1000.0 * c["seconds"] / B for c in res["cases"] if c.get("status") == "ok"]
+            warm = sorted(ms[1:]) if len(ms) > 1 else ms
+            out[name] = {"B": B, "cases": cases, "ms_per_product": warm[len(warm) // 2] if warm else None,
+                         "products_per_s": 1000.0 / warm[len(warm) // 2] if warm else None,
+                         "first_case_ms_per_product": ms[0] if ms else None, "rc": r.returncode}
+        except Exception as e:          # reported, never fatal for the bench line
+            out[name] = {"error": str(e)[:200]}
+        finally:
+            shutil.rmtree(root, ignore_errors=True)
+    out["reference_published"] = {"plain_whole_call_ms": [1.56, 1.67], "batched_B128_ms_per_product": 89.6 / 128,
+                                  "hardware": "RTX PRO 6000 (PCIe)"}
+    return out
 
 
 def autotune_geometries(pkg, args, device, geometries):
@@ -645,6 +696,8 @@ def main():
                     help="parallel branches of the batch graph that launch chains alternate over (with 2 the "
                          "stage events of one chain overlap the other chain's kernels, so the roofline reads low)")
     ap.add_argument("--no-served", dest="served", action="store_false", help="skip the served sweep")
+    ap.add_argument("--no-plugin", dest="plugin", action="store_false",
+                    help="skip timing the plugin harness binaries")
     ap.add_argument("--served-loads", default="0.25,0.5,0.75,0.9",
                     help="offered loads as fractions of the estimated capacity")
     ap.add_argument("--served-seconds", type=float, default=1.5, help="arrival window per offered load")
