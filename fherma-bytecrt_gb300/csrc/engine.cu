@@ -214,11 +214,15 @@ void Context::multiply_pinned(const uint32_t* a, const uint32_t* b, uint32_t* c,
         uint32_t* d = io_dev_[s].as<uint32_t>();
         if (gi >= 2) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
         check(cudaMemcpyAsync(d, a + off, bytes, cudaMemcpyHostToDevice, copy_in_), "input copy");
-        check(cudaMemcpyAsync(d + g * cw, b + off, bytes, cudaMemcpyHostToDevice, copy_in_), "input copy");
         check(cudaEventRecord(ev_in_[s], copy_in_), "event");
         check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
         if (gi >= 2) check(cudaStreamWaitEvent(stream_, ev_out_[s], 0), "slot reuse");
-        chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_);
+        // Operand A first: the device encodes it while operand B comes in.
+        chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_, nullptr, [&] {
+            check(cudaMemcpyAsync(d + g * cw, b + off, bytes, cudaMemcpyHostToDevice, copy_in_), "input copy");
+            check(cudaEventRecord(ev_in_[s], copy_in_), "event");
+            check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
+        });
         check(cudaEventRecord(ev_done_[s], stream_), "event");
         check(cudaStreamWaitEvent(copy_out_, ev_done_[s], 0), "event wait");
         check(cudaMemcpyAsync(c + off, d + 2 * g * cw, bytes, cudaMemcpyDeviceToHost, copy_out_), "output copy");
@@ -307,7 +311,7 @@ void Context::read_profile(double* ms, uint64_t* launches, uint64_t* timed, uint
 }
 
 void Context::chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, uint32_t* ws,
-                    cudaStream_t st, StageTimer* timer) {
+                    cudaStream_t st, StageTimer* timer, const std::function<void()>& between) {
     // Workspace per product: [A planes | B planes]; the product overwrites A.
     const size_t pw = plane_words();
     uint32_t* pa = ws;
@@ -323,14 +327,35 @@ void Context::chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t 
         if (timer) timer->end(st);
         else mark_end(st);
     };
-    begin(kEncode);
-    encode(a, b, pa, pb, stride, count, st);
-    end();
-    // Both operands' column passes in one launch (sets alternate A, B).
-    if (geom().C > 1) {
-        begin(kColForward);
-        check(launch_col_forward(ntt_, pa, pw, 2 * count, st), "column pass launch");
+    if (between) {
+        auto operand = [&](const uint32_t* x, uint32_t* planes) {
+            if (reinterpret_cast<uintptr_t>(x) & 15)
+                throw std::invalid_argument("operand device pointers must be 16-byte aligned");
+            EncodeArgs e = enc_;
+            e.in0 = x; e.in1 = x; e.in_stride = coeff_words();
+            e.out0 = planes; e.out1 = planes; e.out_stride = stride;
+            begin(kEncode);
+            check(launch_encode(e, count, st, 1), "encode launch");
+            end();
+            if (geom().C > 1) {
+                begin(kColForward);
+                check(launch_col_forward(ntt_, planes, stride, count, st), "column pass launch");
+                end();
+            }
+        };
+        operand(a, pa);
+        between();
+        operand(b, pb);
+    } else {
+        begin(kEncode);
+        encode(a, b, pa, pb, stride, count, st);
         end();
+        // Both operands' column passes in one launch (sets alternate A, B).
+        if (geom().C > 1) {
+            begin(kColForward);
+            check(launch_col_forward(ntt_, pa, pw, 2 * count, st), "column pass launch");
+            end();
+        }
     }
     begin(kRow);
     check(launch_row_product(ntt_, pa, stride, pb, stride, pa, stride, count, false, st), "row pass launch");
@@ -446,13 +471,17 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         uint32_t* h = io_host_[s].as<uint32_t>();
         uint32_t* d = io_dev_[s].as<uint32_t>();
         if (gi >= 2) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
+        // Operand A first: the device encodes it while operand B comes in.
         stage_in(reinterpret_cast<char*>(h), reinterpret_cast<char*>(d),
                  reinterpret_cast<const char*>(a + size_t(gi) * g * cw), words * 4);
-        stage_in(reinterpret_cast<char*>(h + g * cw), reinterpret_cast<char*>(d + g * cw),
-                 reinterpret_cast<const char*>(b + size_t(gi) * g * cw), words * 4);
         check(cudaEventRecord(ev_in_[s], copy_in_), "event");
         check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
-        chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_);
+        chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_, nullptr, [&] {
+            stage_in(reinterpret_cast<char*>(h + g * cw), reinterpret_cast<char*>(d + g * cw),
+                     reinterpret_cast<const char*>(b + size_t(gi) * g * cw), words * 4);
+            check(cudaEventRecord(ev_in_[s], copy_in_), "event");
+            check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
+        });
         check(cudaEventRecord(ev_done_[s], stream_), "event");
         check(cudaStreamWaitEvent(copy_out_, ev_done_[s], 0), "event wait");
         const size_t bytes = words * 4;
@@ -463,6 +492,8 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
                                   cudaMemcpyDeviceToHost, copy_out_), "output copy");
             check(cudaEventRecord(piece_ev_[s][k], copy_out_), "event");
         }
+        // While the first group computes, the sink may prepare room for it.
+        if (sink && gi == 0) sink(user, nullptr, words);
     }
     for (uint32_t gi = ngroups >= 2 ? ngroups - 2 : 0; gi < ngroups; ++gi) drain(gi);
     check_status();

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -136,8 +137,12 @@ public:
 
     // One product chain on a caller-provided workspace of >= count products.
     // `timer` (optional) replaces the context's own sampled profiler for this chain.
+    // With `between`, operand A is encoded and column-transformed on its own,
+    // then between() runs on the host (it may bring operand B in and make st
+    // wait for it), then operand B follows: the device works on A while B is
+    // still on its way.
     void chain(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, uint32_t* ws, cudaStream_t st,
-               StageTimer* timer = nullptr);
+               StageTimer* timer = nullptr, const std::function<void()>& between = nullptr);
 
     NttArgs ntt_args() const { return ntt_; }
     const Tuning& tuning() const { return tuning_; }

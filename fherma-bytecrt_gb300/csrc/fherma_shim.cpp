@@ -14,6 +14,12 @@
 #include <exception>
 #include <memory>
 #include <omp.h>
+#include <sys/mman.h>
+#include <unistd.h>
+
+#ifndef MADV_POPULATE_WRITE
+#define MADV_POPULATE_WRITE 23   // Linux 5.14
+#endif
 
 // The owned output vector is built by appending each staged run of the
 // product as it arrives (no zero fill first).  std::vector's append copies
@@ -34,6 +40,27 @@ void parallel_copy(char* dst, const char* src, size_t n) {
     for (int t = 0; t < workers; ++t) {
         const size_t begin = size_t(t) * chunk;
         if (begin < n) __real_memcpy(dst + begin, src + begin, n - begin < chunk ? n - begin : chunk);
+    }
+}
+
+// Faults in the pages of [p, p + n) on all cores (the kernel zero-fills them),
+// so that appending the product later only copies.  Best effort: an older
+// kernel without MADV_POPULATE_WRITE leaves the faults to the copies.
+void populate(void* p, size_t n) {
+    const uintptr_t page = uintptr_t(sysconf(_SC_PAGESIZE));
+    const uintptr_t begin = (uintptr_t(p) + page - 1) & ~(page - 1);
+    const uintptr_t end = (uintptr_t(p) + n) & ~(page - 1);
+    if (end <= begin) return;
+    const size_t pages = (end - begin) / page;
+    const int workers = omp_get_num_procs() < 16 ? omp_get_num_procs() : 16;
+    const size_t per = (pages + workers - 1) / workers;
+#pragma omp parallel for num_threads(workers) schedule(static)
+    for (int t = 0; t < workers; ++t) {
+        const size_t first = size_t(t) * per;
+        if (first < pages) {
+            const size_t count = pages - first < per ? pages - first : per;
+            madvise(reinterpret_cast<void*>(begin + first * page), count * page, MADV_POPULATE_WRITE);
+        }
     }
 }
 
@@ -110,6 +137,10 @@ fherma::Outputs fherma_run(void* state, const fherma::Inputs& in) {
                             [](void* user, const uint32_t* words, size_t n) {
                                 auto* app = static_cast<Append*>(user);
                                 if (app->error) return;
+                                if (!words) {   // the device is busy: fault in the output pages
+                                    populate(app->v->data() + app->v->size(), n * sizeof(uint32_t));
+                                    return;
+                                }
                                 try {
                                     app->v->insert(app->v->end(), words, words + n);
                                 } catch (...) {

@@ -119,9 +119,11 @@ int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_
 /* Like bcg_multiply, but the product ([count][N][L] words) is handed over in
  * order, in consecutive runs, to sink(user, words, n) as each run arrives on
  * the host; `words` is valid only during the call, and the sink must not
- * throw.  For callers that build their own output container (the plugin's
- * owned std::vector) without filling it first.  No counterpart in the
- * reference. */
+ * throw.  Once, while the first products compute, the sink is called with
+ * words == NULL and n = the words that will arrive first: a chance to prepare
+ * the destination (the plugin faults in its output pages then).  For callers
+ * that build their own output container (the plugin's owned std::vector)
+ * without filling it first.  No counterpart in the reference. */
 typedef void (*bcg_sink)(void* user, const uint32_t* words, size_t n);
 int bcg_multiply_sink(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t count, bcg_sink sink,
                       void* user);
