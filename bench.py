@@ -377,7 +377,7 @@ def run_native(args):
     del a_h, b_h, c_h
 
     uneven = run_uneven(pkg, args, stream, local) if args.uneven else None
-    served = run_served(pkg, args, local, value) if args.served else None
+    served = run_served(pkg, args, local, value, e2e_value) if args.served else None
 
     if rank != 0:
         if world > 1:
@@ -544,7 +544,7 @@ def run_uneven(pkg, args, stream, device):
             "chains": info["chains"], "launches": info["launches"], "io_bytes": total_bytes}
 
 
-def run_served(pkg, args, device, batched_value):
+def run_served(pkg, args, device, batched_value, e2e_value=None):
     """Served request loop: seeded Poisson arrivals at swept offered load, 30%
     N=16384/W=434, 40% N=32768/W=868, 30% N=65536/W=1747 over 5 moduli; half
     the requests reuse a resident left operand.  Latency is submission to
@@ -571,7 +571,17 @@ def run_served(pkg, args, device, batched_value):
     shares = np.array([p["share"] for p in points])
     # Work per product relative to N=65536 (N * P, P ~ N * W): capacity estimate for the sweep.
     rel = np.array([(p["n"] * (2 * p["w"] + 20)) / (65536 * 3514.0) for p in points])
-    capacity = batched_value / float((shares * rel).sum())
+    capacity_device = batched_value / float((shares * rel).sum())
+    # Every request also crosses the host link: operand b, operand a unless
+    # resident (half of them), and c.  The batched end-to-end rate gives the
+    # link's bytes/s (3 coefficient arrays per N=65536/W=1747 product).
+    capacity, basis = capacity_device, "device"
+    if e2e_value:
+        link_bytes_s = e2e_value * 3 * 65536 * 55 * 4
+        req_bytes = np.array([2.5 * p["n"] * ((p["w"] + 31) // 32) * 4 for p in points])
+        capacity_link = link_bytes_s / float((shares / shares.sum() * req_bytes).sum())
+        if capacity_link < capacity_device:
+            capacity, basis = capacity_link, "host link"
     loads = [float(x) for x in args.served_loads.split(",")]
     # Alone results for the combinations a request can draw (operand a from pool[0..1]
     # resident or pool[2..3] sent, operand b from pool[4..7]), for verification.
@@ -650,7 +660,8 @@ def run_served(pkg, args, device, batched_value):
     best = max(results, key=lambda r: r["sustained_per_s"])
     return {"workload": "Poisson arrivals; 30% N=16384/W=434, 40% N=32768/W=868, 30% N=65536/W=1747; "
                         "5 moduli (1/2/2); 50% reuse a resident left operand; host buffers (pinned)",
-            "capacity_estimate_per_s": capacity, "sweep": results,
+            "capacity_estimate_per_s": capacity, "capacity_basis": basis,
+            "capacity_device_per_s": capacity_device, "sweep": results,
             "sustained_per_s": best["sustained_per_s"], "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"],
             "memory_budget": stats["memory_budget"], "memory_peak": stats["memory_peak"],
             "rejected": stats["rejected"], "failed": stats["failed"]}
