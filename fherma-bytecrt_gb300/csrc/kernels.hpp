@@ -46,13 +46,13 @@ struct CrtArgs {
 
 struct NttArgs;   // ntt.cuh
 
-// Encode pipeline knobs: B-operand stages (2 or 3) and TMEM chunk buffers (2 or 4).
 // Kernel shape knobs (the autotuner's search space, bcg_context_set_tuning).
 struct Tuning {
     uint32_t crt_tiles = 2;   // 128-row M tiles per CRT CTA: 2 (shared B chunks) or 1 (two CTAs per SM)
     uint32_t crt_persistent = 1;   // 1: persistent warp-specialised CRT (crt_tiles unused); measured
                                    // fastest at N = 16384, 32768 and 65536
-    uint32_t row_rows = 0;    // rows of the row pass per CTA; 0: up to 32
+    uint32_t row_rows = 0;    // rows of the row pass per CTA; 0: 128 (16 elements per thread) or 32,
+                              // halved while the grid holds fewer than four CTAs per SM
     uint32_t crt_gap_fold = 1;   // 1: gap-form q (2^W - gap) reduces by folding; 0: generic reduction
     uint32_t row_local = 0;      // row pass elements per thread: 0 default, 3 (8 elements) or 4 (16, R = 256)
 };

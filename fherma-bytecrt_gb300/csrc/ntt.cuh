@@ -33,7 +33,7 @@ struct NttArgs {
     uint32_t off_tw_lo, off_tw_hi, off_itw_lo, off_itw_hi;
     uint32_t N, P, c_bits, z_bits, Z, H;
     uint32_t R;                // row length of the split N = C * R
-    uint32_t row_rows;         // rows of the row pass per CTA (0: up to 32)
+    uint32_t row_rows;         // rows of the row pass per CTA (0: the launcher's default)
     uint32_t row_local;        // log2 elements per thread in the row pass (0: 4 for R = 256, else 3)
 };
 
