@@ -318,14 +318,23 @@ def run_native(args):
     batch = pkg.Batch(local)
     batch.add(N, W, q, a_dev, b_dev, c_dev, B)
     batch.set_lanes(args.lanes)
-    batch.profile(every=args.profile_every)
+    batch.profile(every=0)            # the timed graph carries no stage events
     for _ in range(args.warmup):
         batch.run(stream.cuda_stream)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         ms = timed(lambda: batch.run(stream.cuda_stream), args.steps)
-    prof = batch.read_profile()       # stage times of the last timed run
     binfo = batch.info()
+    # Stage times for the rooflines: the same graph re-captured with CUDA events
+    # around every stage of every profile_every-th chain (about 1% slower).
+    batch.profile(every=args.profile_every)
+    batch.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    batch.read_profile()
+    for _ in range(max(4, args.steps // 4)):
+        batch.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    prof = batch.read_profile()
     value = world * B * args.steps / (ms / 1000.0)
     c0 = c_dev[0].cpu()
     assert torch.equal(c0, c_dev[DISTINCT].cpu()), "repeated inputs gave different products"
