@@ -24,6 +24,7 @@ BCG_ERR_BUSY = 5
 BCG_ERR_TIMEOUT = 6
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
+SINK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.c_size_t)
 
 
 class BcgError(RuntimeError):
@@ -99,6 +100,7 @@ def lib():
         L.bcg_context_set_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
         L.bcg_context_get_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.bcg_multiply.argtypes = [vp, _u32p, _u32p, _u32p, ctypes.c_uint32]
+        L.bcg_multiply_sink.argtypes = [vp, _u32p, _u32p, ctypes.c_uint32, SINK, vp]
         L.bcg_context_autotune.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(bcg_autotune_report)]
         L.bcg_multiply_device.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
         L.bcg_multiply_device_static.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
@@ -245,6 +247,31 @@ class Multiplier:
         c = np.zeros_like(a)
         _check(lib().bcg_multiply(self._h, _p(a), _p(b), _p(c), count))
         return c
+
+    def multiply_sink(self, a: np.ndarray, b: np.ndarray, sink) -> None:
+        """c = a*b from host buffers, handed over in order as sink(words) calls
+        (a read-only numpy view valid during the call; words=None, first, with
+        the number of words that arrive first, as a chance to prepare)."""
+        a = np.ascontiguousarray(a, dtype=np.uint32)
+        b = np.ascontiguousarray(b, dtype=np.uint32)
+        if a.shape != b.shape or a.size % (self.N * self.L):
+            raise ValueError("operands must be [count][N][L] uint32 of equal shape")
+        count = a.size // (self.N * self.L)
+        errors = []
+
+        def call(user, words, n):
+            try:
+                if not words:
+                    sink(None, int(n))
+                else:
+                    sink(np.ctypeslib.as_array(words, shape=(int(n),)), int(n))
+            except BaseException as e:   # never raise through the C ABI
+                errors.append(e)
+
+        cb = SINK(call)
+        _check(lib().bcg_multiply_sink(self._h, _p(a), _p(b), count, cb, None))
+        if errors:
+            raise errors[0]
 
     def multiply_into(self, a, b, c, count: int):
         """Host buffers given as addresses (e.g. pinned torch tensors): c = a*b, synchronous."""

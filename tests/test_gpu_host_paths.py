@@ -1,0 +1,104 @@
+"""Host-buffer paths through the C ABI at sizes that take several staging
+groups: pageable buffers (bcg_multiply: direct DMA of the inputs where the
+GPU reads host page tables, staged output pieces), pinned buffers (direct DMA
+both ways), and the sink entry point the plugin uses (bcg_multiply_sink: the
+product in order, in pieces).  Every product equals the device-resident path,
+and a few are checked against the oracle."""
+import numpy as np
+import pytest
+
+from conftest import package
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def operands(pkg, q, N, count, seed):
+    a = np.stack([pkg.inputs.uniform(q, N, seed + i) for i in range(count)])
+    b = np.stack([pkg.inputs.uniform(q, N, seed + 500 + i) for i in range(count)])
+    return a, b
+
+
+def device_products(m, a, b):
+    da = torch.from_numpy(a.view(np.int32)).cuda()
+    db = torch.from_numpy(b.view(np.int32)).cuda()
+    dc = torch.empty_like(da)
+    m.multiply_device(da, db, dc, a.shape[0])
+    m.synchronize()
+    return dc.cpu().numpy().view(np.uint32)
+
+
+# (N, W, count): the last two take three host groups (the staging groups hold
+# about 128 MiB of operands: 4 products at N=65536, 71 at N=16384).
+CASES = [(4096, 868, 5), (65536, 1747, 9), (16384, 434, 150)]
+
+
+@pytest.mark.parametrize("N,W,count", CASES)
+def test_pageable_host_buffers(N, W, count):
+    pkg = package()
+    q = pkg.inputs.modulus(W, 31)
+    m = pkg.Multiplier(N, W, q)
+    a, b = operands(pkg, q, N, count, 100)
+    got = m.multiply(a, b)
+    assert np.array_equal(got, device_products(m, a, b))
+    o = O.Oracle(N, W, q)
+    for i in (0, count - 1):
+        assert np.array_equal(got[i], o.multiply(a[i], b[i])), i
+    m.close()
+
+
+@pytest.mark.parametrize("N,W,count", CASES)
+def test_pinned_host_buffers(N, W, count):
+    pkg = package()
+    q = pkg.inputs.modulus(W, 32)
+    m = pkg.Multiplier(N, W, q)
+    a, b = operands(pkg, q, N, count, 200)
+    ta = torch.from_numpy(a.view(np.int32)).pin_memory()
+    tb = torch.from_numpy(b.view(np.int32)).pin_memory()
+    tc = torch.zeros_like(ta).pin_memory()
+    m.multiply_into(ta, tb, tc, count)
+    assert np.array_equal(tc.numpy().view(np.uint32), device_products(m, a, b))
+    m.close()
+
+
+@pytest.mark.parametrize("N,W,count", CASES)
+def test_sink_pieces_arrive_in_order(N, W, count):
+    pkg = package()
+    q = pkg.inputs.gap_modulus(W, 12345) if W > 70 else pkg.inputs.modulus(W, 33)
+    m = pkg.Multiplier(N, W, q)
+    a, b = operands(pkg, q, N, count, 300)
+    calls, pieces = [], []
+
+    def sink(words, n):
+        calls.append((words is None, n))
+        if words is not None:
+            assert words.shape == (n,) and n <= (4 << 20) // 4
+            pieces.append(words.copy())
+
+    m.multiply_sink(a, b, sink)
+    # One preparation call first, with the words of the first group.
+    assert calls[0][0] and 0 < calls[0][1] <= a.size
+    assert sum(1 for prep, _ in calls if prep) == 1
+    got = np.concatenate(pieces).reshape(a.shape)
+    assert np.array_equal(got, device_products(m, a, b))
+    m.close()
+
+
+def test_sink_exception_is_reraised():
+    pkg = package()
+    N, W = 1024, 200
+    q = pkg.inputs.modulus(W, 34)
+    m = pkg.Multiplier(N, W, q)
+    a, b = operands(pkg, q, N, 2, 400)
+
+    def sink(words, n):
+        if words is not None:
+            raise RuntimeError("caller-side failure")
+
+    with pytest.raises(RuntimeError, match="caller-side failure"):
+        m.multiply_sink(a, b, sink)
+    # The context stays usable.
+    assert np.array_equal(m.multiply(a, b), device_products(m, a, b))
+    m.close()
