@@ -121,6 +121,48 @@ def make_inputs(pkg, seed_base: int):
     return q, a, b
 
 
+def host_link(h_in, d_in, h_out, d_out, reps: int = 3) -> dict:
+    """Copy-engine rates of the host link between pinned host memory and this
+    GPU: H2D alone, D2H alone, and both directions at once (GB/s each way).
+    The buffers are the e2e step's own pinned and device tensors, so the copies
+    rewrite them with the contents they already hold."""
+    import torch
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(pairs) -> float:
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s_in)
+        s_out.wait_stream(s_in)
+        for _ in range(reps):
+            for dst, src, st in pairs:
+                with torch.cuda.stream(st):
+                    dst.copy_(src, non_blocking=True)
+        s_in.wait_stream(s_out)
+        e1.record(s_in)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1000.0 / reps
+
+    nb_in, nb_out = h_in.numel() * h_in.element_size(), h_out.numel() * h_out.element_size()
+    t_in = timed([(d_in, h_in, s_in)])
+    t_out = timed([(h_out, d_out, s_out)])
+    t_both = timed([(d_in, h_in, s_in), (h_out, d_out, s_out)])
+    return {"h2d_gbs": nb_in / t_in / 1e9, "d2h_gbs": nb_out / t_out / 1e9,
+            "both_gbs": (nb_in + nb_out) / t_both / 1e9, "bytes": [nb_in, nb_out],
+            "method": "cudaMemcpyAsync on two streams, pinned host memory, %d reps" % reps}
+
+
+def link_bound(link: dict, in_bytes: int, out_bytes: int) -> float:
+    """Products/s the host link allows when each product moves in_bytes in and
+    out_bytes out: while both directions run each gets half of the measured
+    two-way rate; the rest of the larger direction runs alone."""
+    both = link["both_gbs"] * 1e9 / 2
+    shared = min(in_bytes, out_bytes)
+    rest_in, rest_out = in_bytes - shared, out_bytes - shared
+    t = shared / both + rest_in / (link["h2d_gbs"] * 1e9) + rest_out / (link["d2h_gbs"] * 1e9)
+    return 1.0 / t
+
+
 def tile_to(t, count):
     import torch
     reps = (count + t.shape[0] - 1) // t.shape[0]
@@ -383,6 +425,7 @@ def run_native(args):
     for i in range(plain_iters):
         m.multiply_into(a_h[i % DISTINCT], b_h[i % DISTINCT], c_h[i % DISTINCT], 1)
     plain_e2e_ms = 1000 * (time.perf_counter() - t0) / plain_iters
+    link = host_link(a_h, a_dev, c_h, c_dev)
     del a_h, b_h, c_h
 
     uneven = run_uneven(pkg, args, stream, local) if args.uneven else None
@@ -430,7 +473,10 @@ def run_native(args):
                    "autotune": tuning,
                    "l2": "inputs larger than L2 (3.7 GB per step), no flush", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": 2 * B * N * L * 4,
-                "d2h_bytes_per_step": B * N * L * 4, "api": "bcg_multiply (host buffers, pinned)"},
+                "d2h_bytes_per_step": B * N * L * 4, "api": "bcg_multiply (host buffers, pinned)",
+                "link_bound": link_bound(link, 2 * N * L * 4, N * L * 4),
+                "link_frac": e2e_value / world / link_bound(link, 2 * N * L * 4, N * L * 4),
+                "host_link": link},
         "stream_launch": {"products_per_s": stream_value, "ms_per_step": stream_ms / max(3, args.steps // 2)},
         "plain": {"device_ms_per_product": plain_ms, "device_products_per_s": 1000.0 / plain_ms,
                   "e2e_ms_per_product": plain_e2e_ms, "e2e_products_per_s": 1000.0 / plain_e2e_ms,
