@@ -4,8 +4,9 @@
 //   warp 0      loader: per K chunk, one bulk copy of the weight-digit chunk and
 //               the 8 t_j plane rows of the tile into a stage (6 stages);
 //   warp 1      MMA: tcgen05 kind::f16 into one of two TMEM accumulators;
-//   warps 2-9   producers, two per row: each turns 4 of the chunk's 8 terms
-//               into balanced fp16 digits and keeps a partial alpha sum;
+//   warps 2-9   producers in two groups of four warps that take alternate
+//               chunks: each thread turns its row's 8 terms of the chunk into
+//               balanced fp16 digits and keeps its group's partial alpha sum;
 //   warps 10-13 epilogue: carry chain, reduction mod q, one bulk store per tile.
 // The two accumulators let the epilogue of tile i run while tile i+1 goes
 // through the MMA loop; the epilogue hands its accumulator back as soon as
@@ -14,8 +15,8 @@
 //
 // alpha is the nearest integer to sum_j t_j / p_j; the plan's bound
 // (|c/Prod| < 1/4 and P*gamma_(P+4) < 1/4) makes every summation order give
-// that integer, so the two partial sums per row (each in the reference's
-// fp32 round-to-nearest arithmetic) give the reference's alpha.
+// that integer, so the two groups' partial sums per row (each in the
+// reference's fp32 round-to-nearest arithmetic) give the reference's alpha.
 //
 // Every wait is bounded.  Roles never leave their loops early: once a wait
 // gives up (ok = false) a thread skips its work but still reaches every named
@@ -83,7 +84,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
     if (threadIdx.x == 0) {
         for (uint32_t i = 0; i < kPStages; ++i) {
             mbar_init(&ctl->bfull[i], 1);
-            mbar_init(&ctl->afull[i], kProdThreads);
+            mbar_init(&ctl->afull[i], kProdThreads / 2);   // one producer group per chunk
             mbar_init(&ctl->sempty[i], 1);
         }
         for (uint32_t b = 0; b < 2; ++b) {
@@ -175,9 +176,12 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
         }
         __syncwarp();
     } else if (warp < kEpiWarp0) {
-        // ---- producers: row = thread % 128, half = which 4 terms of each chunk.
+        // ---- producers: two groups of four warps take alternate chunks (g even
+        // or odd, so each group owns every other stage); in a group, thread =
+        // row, all 8 terms of the chunk.  One group's chunk latency (wait,
+        // loads, conversion, fence, arrival) overlaps the other's.
         const uint32_t pt = threadIdx.x - kProdWarp0 * 32;
-        const uint32_t row = pt % kTileRows, half = pt / kTileRows;
+        const uint32_t row = pt % kTileRows, grp = pt / kTileRows;
         bool ok = true;
         uint32_t g = 0;
         for (uint32_t job = blockIdx.x; job < njobs; job += gridDim.x) {
@@ -185,38 +189,48 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             const bool valid = row < min(kTileRows, N - row0);
             float acc = 0.0f;
             for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
+                const bool mine = (g & 1u) == grp;
+                if (kc == alpha_chunk && !mine) {
+                    // Every term below P lies in a chunk before this one: hand
+                    // the partial sum to the group that builds alpha's digits.
+                    // Both groups pass this barrier once per tile (a blocking
+                    // sync on both sides keeps the pairing exact even when
+                    // waits have given up and threads run ahead).
+                    ctl->alpha_part[grp][row] = acc;
+                    named_sync(2, kProdThreads);
+                }
+                if (!mine) continue;
                 const uint32_t s = g % kPStages;
                 if (ok) ok = mbar_wait(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status);
                 const uint32_t kl = chunk_k(a.k_total, kc);
                 const uint32_t* ts = stageT(s) + row;
-                uint32_t t[4];
+                uint32_t t[kTermsPerChunk];
 #pragma unroll
-                for (uint32_t jj = 0; jj < 4; ++jj) {
-                    const uint32_t u = kc * kTermsPerChunk + 4 * half + jj;
-                    t[jj] = (ok && u < P && valid) ? ts[(4 * half + jj) * kTileRows] : 0u;
+                for (uint32_t jj = 0; jj < kTermsPerChunk; ++jj) {
+                    const uint32_t u = kc * kTermsPerChunk + jj;
+                    t[jj] = (ok && u < P && valid) ? ts[jj * kTileRows] : 0u;
                 }
 #pragma unroll
-                for (uint32_t jj = 0; jj < 4; ++jj) {
-                    const uint32_t u = kc * kTermsPerChunk + 4 * half + jj;
+                for (uint32_t jj = 0; jj < kTermsPerChunk; ++jj) {
+                    const uint32_t u = kc * kTermsPerChunk + jj;
                     if (u < P) acc = __fadd_rn(acc, __fmul_rn(__uint2float_rn(t[jj]), a.invp[u]));
                 }
                 uint32_t alpha = 0;
                 if (kc == alpha_chunk) {
-                    // alpha = round(partial_0 + partial_1), the digits of term P.
-                    ctl->alpha_part[half][row] = acc;
+                    // alpha = round(own partial + the other group's), the digits of term P.
                     named_sync(2, kProdThreads);
-                    alpha = __float2uint_rn(__fadd_rn(ctl->alpha_part[0][row], ctl->alpha_part[1][row]));
+                    alpha = __float2uint_rn(__fadd_rn(acc, ctl->alpha_part[grp ^ 1u][row]));
                 }
                 if (ok) {
                     uint8_t* tileA = stageA(s);
 #pragma unroll
-                    for (uint32_t pp = 0; pp < 2; ++pp) {
-                        const uint32_t kpos = 8 * (2 * half + pp);         // first of this pair's 8 digits
+                    for (uint32_t pp = 0; pp < kTermsPerChunk / 2; ++pp) {
+                        const uint32_t kpos = 8 * pp;                      // first of this pair's 8 digits
                         if (kpos >= kl) break;
                         uint32_t h[4];
 #pragma unroll
                         for (uint32_t hh = 0; hh < 2; ++hh) {
-                            const uint32_t u = kc * kTermsPerChunk + 4 * half + 2 * pp + hh;
+                            const uint32_t u = kc * kTermsPerChunk + 2 * pp + hh;
                             const uint32_t tb = (u == P ? alpha : t[2 * pp + hh]) + 0x808080u;
                             const bool live = u <= P && valid;
                             h[2 * hh] = live ? bytes01_to_half2(tb, kBias128x2) : 0u;
