@@ -137,12 +137,21 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
     asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
                  :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+// suspend_ns > 0: a thread whose phase has not completed may sleep in
+// hardware for up to that long per poll (it wakes when the phase completes),
+// so many waiting warps do not keep the shared-memory pipe busy with polls.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity, uint32_t suspend_ns = 0) {
     uint32_t done;
-    asm volatile("{\n\t.reg .pred p;\n\t"
-                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    if (suspend_ns)
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(smem_u32(bar)), "r"(parity), "r"(suspend_ns) : "memory");
+    else
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
     return done != 0;
 }
 // Bounded wait.  Returns false (and records the timeout) if the phase with the
@@ -150,11 +159,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // the CTA already gave up (abort flag in shared memory).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
                                           volatile uint32_t* abort_flag,
-                                          uint32_t* status) {
-    if (mbar_try_wait(bar, parity)) return true;
+                                          uint32_t* status, uint32_t suspend_ns = 0) {
+    if (mbar_try_wait(bar, parity, suspend_ns)) return true;
     const uint64_t start = global_ns();
     for (uint32_t spin = 0;; ++spin) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait(bar, parity, suspend_ns)) return true;
         if ((spin & 63) == 0) {
             if (*abort_flag) return false;
             if (global_ns() - start > kWaitLimitNs) {
@@ -169,11 +178,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
 // Waits for this thread's own asynchronous work (copies, MMAs) to land before
 // the CTA leaves: bounded by the same limit, but not cut short by the abort
 // flag (an aborted CTA must still not exit with its copies in flight).
-__device__ __forceinline__ bool mbar_wait_own(uint64_t* bar, uint32_t parity, uint32_t* status) {
-    if (mbar_try_wait(bar, parity)) return true;
+__device__ __forceinline__ bool mbar_wait_own(uint64_t* bar, uint32_t parity, uint32_t* status,
+                                              uint32_t suspend_ns = 0) {
+    if (mbar_try_wait(bar, parity, suspend_ns)) return true;
     const uint64_t start = global_ns();
     for (uint32_t spin = 0;; ++spin) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait(bar, parity, suspend_ns)) return true;
         if ((spin & 63) == 0 && global_ns() - start > kWaitLimitNs) {
             atomicExch(status, kStatusWaitTimeout);
             return false;

@@ -39,6 +39,9 @@ constexpr uint32_t kProdThreads = 8 * 32;
 constexpr uint32_t kEpiThreads = 4 * 32;
 constexpr uint32_t kPThreads = 14 * 32;
 constexpr uint32_t kAccCols = 256;             // one accumulator (NC <= 256 fp32 columns)
+// Waiting threads sleep up to this long per poll (14 warps wait at once; the
+// epilogue's waits last a whole tile).  CRT 20.0 -> 18.9 us per product at N=65536.
+constexpr uint32_t kSuspendNs = 20000;
 
 struct PSmem {
     uint64_t bfull[kPStages], afull[kPStages], sempty[kPStages];
@@ -117,7 +120,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                                         (a.terms_tiled ? size_t(row0) * P : size_t(row0));
                 for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
                     const uint32_t s = g % kPStages;
-                    if (g >= kPStages && !mbar_wait(&ctl->sempty[s], ((g / kPStages) - 1) & 1, abort_flag, a.status)) {
+                    if (g >= kPStages && !mbar_wait(&ctl->sempty[s], ((g / kPStages) - 1) & 1, abort_flag, a.status, kSuspendNs)) {
                         ok = false;
                         break;
                     }
@@ -137,7 +140,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             // Let the last copy into every stage land before the CTA can exit.
             for (uint32_t back = 1; back <= kPStages && back <= g; ++back) {
                 const uint32_t gg = g - back;
-                mbar_wait_own(&ctl->bfull[gg % kPStages], (gg / kPStages) & 1, a.status);
+                mbar_wait_own(&ctl->bfull[gg % kPStages], (gg / kPStages) & 1, a.status, kSuspendNs);
             }
         }
         __syncwarp();
@@ -148,14 +151,14 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             uint32_t g = 0, it = 0;
             for (uint32_t job = blockIdx.x; ok && job < njobs; job += gridDim.x, ++it) {
                 const uint32_t buf = it & 1;
-                if (it >= 2 && !mbar_wait(&ctl->accempty[buf], ((it / 2) - 1) & 1, abort_flag, a.status)) {
+                if (it >= 2 && !mbar_wait(&ctl->accempty[buf], ((it / 2) - 1) & 1, abort_flag, a.status, kSuspendNs)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
                     const uint32_t s = g % kPStages;
-                    if (!mbar_wait(&ctl->afull[s], (g / kPStages) & 1, abort_flag, a.status)) {
+                    if (!mbar_wait(&ctl->afull[s], (g / kPStages) & 1, abort_flag, a.status, kSuspendNs)) {
                         ok = false;
                         break;
                     }
@@ -172,7 +175,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             }
             // Every MMA issued by this thread has retired once mma_done completes.
             mma_commit(&ctl->mma_done);
-            mbar_wait_own(&ctl->mma_done, 0, a.status);
+            mbar_wait_own(&ctl->mma_done, 0, a.status, kSuspendNs);
         }
         __syncwarp();
     } else if (warp < kEpiWarp0) {
@@ -201,7 +204,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                 }
                 if (!mine) continue;
                 const uint32_t s = g % kPStages;
-                if (ok) ok = mbar_wait(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status);
+                if (ok) ok = mbar_wait(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status, kSuspendNs);
                 const uint32_t kl = chunk_k(a.k_total, kc);
                 const uint32_t* ts = stageT(s) + row;
                 uint32_t t[kTermsPerChunk];
@@ -258,7 +261,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             const uint32_t prod = job / ntiles, row0 = (job % ntiles) * kTileRows;
             const uint32_t rows = min(kTileRows, N - row0);
             const bool valid = row < rows;
-            if (ok) ok = mbar_wait(&ctl->accfull[buf], (it / 2) & 1, abort_flag, a.status);
+            if (ok) ok = mbar_wait(&ctl->accfull[buf], (it / 2) & 1, abort_flag, a.status, kSuspendNs);
             uint32_t z[LT ? LT : 1];
             int64_t top = 0;
             if (ok) {
