@@ -19,11 +19,14 @@
 // so that one group's byte-power matrix stays resident in shared memory for
 // the whole launch (one bulk copy per CTA); CTAs of group g loop over all
 // 128-row tiles of all operands and products.  A tiles and TMEM accumulators
-// are double buffered: builders (warps 0-3, thread = row) fill tile i+1 while
-// the MMA of tile i runs and the epilogue warps drain tile i-1.  Warp roles:
-//   warps 0-3    A-tile builders (balanced fp16 digits of one row each)
-//   warps 4-19   epilogue, four warps per TMEM lane quarter, each a quarter of the columns
-//   warp 20      TMEM allocation, B load, MMA issue (one thread)
+// are double buffered: builders fill tile i+1 while the MMA of tile i runs
+// and the epilogue warps drain tile i-1.  Warp roles:
+//   warps 0-7    A-tile builders in two groups, one per A buffer (thread = row:
+//                balanced fp16 digits of one row each); a group issues its
+//                buffer's input copy as soon as the MMA has released it, so
+//                one buffer's copy overlaps the other's conversion
+//   warps 8-23   epilogue, four warps per TMEM lane quarter, each a quarter of the columns
+//   warp 24      TMEM allocation, B load, MMA issue (one thread)
 // The epilogue bounds the job rate (per-job globaltimer traces: the MMA waits
 // for the accumulator the epilogue hands back); four warps per quarter
 // rather than three measured 3.6% faster at N = 65536.
@@ -34,7 +37,8 @@ namespace bcg {
 namespace {
 
 constexpr uint32_t kTileRows = 128;
-constexpr uint32_t kBuildWarps = 4;
+constexpr uint32_t kBuildGroupWarps = 4;   // one builder thread per tile row
+constexpr uint32_t kBuildWarps = 2 * kBuildGroupWarps;   // one builder group per A buffer
 constexpr uint32_t kEpiPerQuarter = 4;      // epilogue warps per TMEM lane quarter
 constexpr uint32_t kEpiWarps = 4 * kEpiPerQuarter;
 constexpr uint32_t kCtlWarp = kBuildWarps + kEpiWarps;
@@ -171,10 +175,11 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
         // contiguous: one bulk copy stages them in the tail of the A buffer
         // being filled; every builder reads its row before any digit is
         // written (named barrier), so the in-place conversion is race free.
-        const uint32_t r = threadIdx.x;
+        const uint32_t grp = warp / kBuildGroupWarps;           // = the A buffer this group fills
+        const uint32_t r = threadIdx.x - grp * kBuildGroupWarps * 32;
         const uint32_t stage_off = (tile_bytes - kTileRows * L * 4) & ~15u;
-        uint32_t ii = 0;
-        for (uint32_t job = slot; job < njobs; job += nslots, ++ii) {
+        uint32_t ii = grp;
+        for (uint32_t job = slot + grp * nslots; job < njobs; job += 2 * nslots, ii += 2) {
             const uint32_t s = ii & 1, use = ii >> 1;
             if (ii >= 2 && !mbar_wait(&ctl->aempty[s], (use - 1) & 1, abort_flag, a.status)) break;
             const uint32_t tile = job % ntiles, operand = (job / ntiles) % a.operands;
@@ -205,7 +210,9 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
                 if (!LT && l >= L) break;
                 w[l] = (valid && ok_in) ? staged[r * L + l] : 0u;
             }
-            asm volatile("bar.sync 1, %0;" :: "r"(kBuildWarps * 32) : "memory");
+            // One named barrier per builder group (ids 1 and 2).
+            if (grp == 0) asm volatile("bar.sync 1, %0;" :: "r"(kBuildGroupWarps * 32) : "memory");
+            else asm volatile("bar.sync 2, %0;" :: "r"(kBuildGroupWarps * 32) : "memory");
             if (!ok_in) break;
             if (valid) {
                 digits_row<LT>(buf, r, w, L, K);
