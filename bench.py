@@ -472,6 +472,13 @@ def run_native(args):
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
     stage_us = {s: 1000 * per_launch[s] * launches[s] / B for s in per_launch}
     all_rooflines = rooflines(info, stage_us, sm_count, clock["sm_mhz"] or 2070.0)
+    # The NTT passes are bound by integer multiplies, not HBM: for them the INT32 issue rate (warp
+    # instructions x 32 / time against 4 warp instructions per clock per SM) sits beside the HBM figure.
+    dom = all_rooflines["stages"].get(dominant, {})
+    if dominant in ("column", "row", "column_inverse") and "issue_frac" in dom:
+        roofline["binding"] = {"resource": "INT32 issue", "frac": dom["issue_frac"],
+                               "achieved_tinst_per_s": dom["issue_tinst_per_s"],
+                               "peak_tinst_per_s": all_rooflines["issue_peak_tinst_per_s"]}
     cpu = cpu_baseline(pkg, q, a_np, b_np, sample=args.cpu_sample) if args.cpu_sample > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "products/s", "n_gpus": world, "steps": args.steps,
