@@ -43,6 +43,10 @@ constexpr uint32_t kEpiPerQuarter = 4;      // epilogue warps per TMEM lane quar
 constexpr uint32_t kEpiWarps = 4 * kEpiPerQuarter;
 constexpr uint32_t kCtlWarp = kBuildWarps + kEpiWarps;
 constexpr uint32_t kEncThreads = (kCtlWarp + 1) * 32;
+// The MMA-issuing thread sleeps up to this long per mbarrier poll (30.65 ->
+// 30.49 us per product at N=65536); the builders' and epilogue's waits
+// measured slower with it and keep polling.
+constexpr uint32_t kCtlSuspendNs = 20000;
 
 struct EncodeSmem {
     uint64_t bfull, afull[2], aempty[2], accfull[2], accempty[2], infull[2];
@@ -145,15 +149,15 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             const uint32_t bbytes = gcols * K * 2;
             mbar_arrive_expect_tx(&ctl->bfull, bbytes);
             bulk_load(bres, a.enc_b + size_t(col0) * K, bbytes, &ctl->bfull);
-            bool ok = mbar_wait(&ctl->bfull, 0, abort_flag, a.status);
+            bool ok = mbar_wait(&ctl->bfull, 0, abort_flag, a.status, kCtlSuspendNs);
             const uint32_t sbo = (K / 8) * 128;
             const uint32_t idesc = idesc_f16_f32(kTileRows, gcols);
             const uint32_t b_addr = smem_u32(bres);
             uint32_t ii = 0;
             for (uint32_t job = slot; ok && job < njobs; job += nslots, ++ii) {
                 const uint32_t s = ii & 1, use = ii >> 1;
-                ok = mbar_wait(&ctl->afull[s], use & 1, abort_flag, a.status);
-                if (ok && ii >= 2) ok = mbar_wait(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status);
+                ok = mbar_wait(&ctl->afull[s], use & 1, abort_flag, a.status, kCtlSuspendNs);
+                if (ok && ii >= 2) ok = mbar_wait(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status, kCtlSuspendNs);
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t a_addr = smem_u32(tiles + s * tile_bytes);
@@ -166,7 +170,7 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             // Drain the last commits before TMEM is freed.
             for (uint32_t back = 1; back <= 2 && back <= ii; ++back) {
                 const uint32_t jj = ii - back;
-                mbar_wait(&ctl->aempty[jj & 1], (jj >> 1) & 1, abort_flag, a.status);
+                mbar_wait(&ctl->aempty[jj & 1], (jj >> 1) & 1, abort_flag, a.status, kCtlSuspendNs);
             }
         }
         __syncwarp();
