@@ -162,13 +162,21 @@ def best_link(x: dict, y: dict) -> dict:
 
 
 def link_bound(link: dict, in_bytes: int, out_bytes: int) -> float:
-    """Products/s the host link allows when each product moves in_bytes in and
-    out_bytes out: while both directions run each gets half of the measured
-    two-way rate; the rest of the larger direction runs alone."""
+    """Products/s the host link allows at most when each product moves in_bytes
+    in and out_bytes out: no schedule beats the slowest of the three measured
+    capacities (H2D alone, D2H alone, both directions together)."""
+    t = max(in_bytes / (link["h2d_gbs"] * 1e9), out_bytes / (link["d2h_gbs"] * 1e9),
+            (in_bytes + out_bytes) / (link["both_gbs"] * 1e9))
+    return 1.0 / t
+
+
+def link_model_even_split(link: dict, in_bytes: int, out_bytes: int) -> float:
+    """Products/s if, while both directions run, each gets half of the two-way
+    rate and the rest of the larger direction then runs alone (how the probe's
+    equal-size two-way copies behaved); a model, not a bound."""
     both = link["both_gbs"] * 1e9 / 2
     shared = min(in_bytes, out_bytes)
-    rest_in, rest_out = in_bytes - shared, out_bytes - shared
-    t = shared / both + rest_in / (link["h2d_gbs"] * 1e9) + rest_out / (link["d2h_gbs"] * 1e9)
+    t = shared / both + (in_bytes - shared) / (link["h2d_gbs"] * 1e9) + (out_bytes - shared) / (link["d2h_gbs"] * 1e9)
     return 1.0 / t
 
 
@@ -495,6 +503,7 @@ def run_native(args):
                 "d2h_bytes_per_step": B * N * L * 4, "api": "bcg_multiply (host buffers, pinned)",
                 "link_bound": link_bound(link, 2 * N * L * 4, N * L * 4),
                 "link_frac": e2e_value / world / link_bound(link, 2 * N * L * 4, N * L * 4),
+                "link_model_even_split": link_model_even_split(link, 2 * N * L * 4, N * L * 4),
                 "host_link": link},
         "stream_launch": {"products_per_s": stream_value, "ms_per_step": stream_ms / max(3, args.steps // 2)},
         "plain": {"device_ms_per_product": plain_ms, "device_products_per_s": 1000.0 / plain_ms,
