@@ -189,9 +189,12 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
         __syncwarp();
     } else if (warp < kEpiWarp0) {
         // ---- producers: two groups of four warps take alternate chunks (g even
-        // or odd, so each group owns every other stage); in a group, thread =
-        // row, all 8 terms of the chunk.  One group's chunk latency (wait,
-        // loads, conversion, fence, arrival) overlaps the other's.
+        // or odd); in a group, thread = row, all 8 terms of the chunk.  One
+        // group's chunk latency (wait, loads, conversion, fence, arrival)
+        // overlaps the other's.  With an odd stage count a stage passes from
+        // one group to the other between uses; a group still never falls two
+        // phases behind a stage's bfull, because refilling the stage needs the
+        // MMA of this group's chunk, hence this group's arrival.
         const uint32_t pt = threadIdx.x - kProdWarp0 * 32;
         const uint32_t row = pt % kTileRows, grp = pt / kTileRows;
         bool ok = true;
