@@ -385,7 +385,9 @@ def run_native(args):
         ms = timed(lambda: batch.run(stream.cuda_stream), args.steps)
     binfo = batch.info()
     # Stage times for the rooflines: the same graph re-captured with CUDA events
-    # around every stage of every profile_every-th chain (about 1% slower).
+    # around every stage of every profile_every-th chain (about 1% slower), on
+    # one branch so that each stage's events bracket that stage's kernels only.
+    batch.set_lanes(1)
     batch.profile(every=args.profile_every)
     batch.run(stream.cuda_stream)
     torch.cuda.synchronize()
@@ -787,8 +789,8 @@ def main():
     ap.add_argument("--no-uneven", dest="uneven", action="store_false", help="skip the uneven 96-product batch")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="keep the default kernel shapes")
     ap.add_argument("--lanes", type=int, default=1, choices=(1, 2),
-                    help="parallel branches of the batch graph that launch chains alternate over (with 2 the "
-                         "stage events of one chain overlap the other chain's kernels, so the roofline reads low)")
+                    help="parallel branches of the timed batch graph that launch chains alternate over (the "
+                         "profiled pass for the rooflines always runs one branch)")
     ap.add_argument("--no-served", dest="served", action="store_false", help="skip the served sweep")
     ap.add_argument("--no-plugin", dest="plugin", action="store_false",
                     help="skip timing the plugin harness binaries")
