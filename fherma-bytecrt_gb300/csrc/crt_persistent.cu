@@ -63,8 +63,22 @@ __host__ __device__ constexpr uint32_t zstage_bytes_for(uint32_t L) {
 size_t smem_bytes_for(uint32_t NC, uint32_t L, uint32_t stages) {
     return size_t(stages) * stage_bytes_for(NC) + zstage_bytes_for(L) + sizeof(PSmem) + 1024;
 }
+// The device's opt-in shared memory per block (227 KB on GB300), read once.
+size_t smem_optin_bytes() {
+    static int bytes = 0;
+    if (!bytes) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0) {
+            cudaGetLastError();
+            v = 227 * 1024;
+        }
+        bytes = v;
+    }
+    return size_t(bytes);
+}
 uint32_t stages_for(uint32_t NC, uint32_t L) {
-    return smem_bytes_for(NC, L, kMaxStages) <= size_t(227) * 1024 ? kMaxStages : kMaxStages - 1;
+    return smem_bytes_for(NC, L, kMaxStages) <= smem_optin_bytes() ? kMaxStages : kMaxStages - 1;
 }
 
 __device__ __forceinline__ void named_sync(uint32_t id, uint32_t threads) {
