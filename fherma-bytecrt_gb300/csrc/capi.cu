@@ -127,6 +127,9 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
             bcg::Tuning t = c.tuning();
             t.row_rows = uint32_t(value);
             c.set_tuning(t);
+        } else if (k == "wait_limit_ns") {
+            require(value >= 0 && value <= 60000000000ll, "wait_limit_ns must be in [0, 6e10]");
+            c.set_wait_limit_ns(uint64_t(value));
         } else {
             throw std::invalid_argument("unknown tuning knob: " + k);
         }
@@ -146,6 +149,7 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         else if (k == "crt_gap_fold") *value = c.tuning().crt_gap_fold;
         else if (k == "row_local") *value = c.tuning().row_local;
         else if (k == "gap") *value = c.plan().gap;
+        else if (k == "wait_limit_ns") *value = int64_t(c.wait_limit_ns());
         else throw std::invalid_argument("unknown tuning knob: " + k);
     });
 }

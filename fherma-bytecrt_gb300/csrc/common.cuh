@@ -7,6 +7,15 @@
 // device status word and returns false; the kernel then skips its remaining
 // work, drains what it started and frees its TMEM, so the CUDA context stays
 // usable and the host reports the status.
+//
+// Two kinds of wait:
+//   mbar_wait      waits for another role's arrival (a producer's tile, the
+//                  MMA's commit).  Its limit is a kernel argument (the
+//                  context's wait limit, 2 s by default) and it also gives up
+//                  as soon as another thread of the CTA has given up;
+//   mbar_wait_own  waits for this thread's own asynchronous work (its bulk
+//                  copies, its MMAs) before the CTA may leave or free TMEM.
+//                  It keeps the fixed 2 s limit and ignores the abort flag.
 #pragma once
 
 #include <cstdint>
@@ -154,19 +163,45 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity, ui
                      : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
     return done != 0;
 }
-// Bounded wait.  Returns false (and records the timeout) if the phase with the
-// given parity did not complete within kWaitLimitNs, or if another thread of
-// the CTA already gave up (abort flag in shared memory).
+// Non-blocking test of the phase with the given parity.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return done != 0;
+}
+
+// Bounded wait for another role's arrival.  Returns false (and records the
+// timeout) if the phase with the given parity did not complete within
+// limit_ns, or if another thread of the CTA already gave up (abort flag in
+// shared memory).  Threads of one warp can see different outcomes (one sees
+// the phase complete, another the abort flag): vote before a warp-collective
+// step.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
                                           volatile uint32_t* abort_flag,
-                                          uint32_t* status, uint32_t suspend_ns = 0) {
+                                          uint32_t* status, uint64_t limit_ns, uint32_t suspend_ns = 0) {
+    if (limit_ns < 1000ull) {
+        // Finer than %globaltimer resolves: one non-blocking test (a blocking
+        // poll may suspend the thread long enough to cover a short wait).
+        if (mbar_test_wait(bar, parity)) return true;
+        if (!*abort_flag) {
+            *abort_flag = 1;
+            atomicExch(status, kStatusWaitTimeout);
+        }
+        return false;
+    }
+    // The clock is read every 64 polls and a poll may suspend the thread (for
+    // up to suspend_ns, or a time the hardware chooses), so a wait can overrun
+    // its limit by that much: the limit is a lower bound.
     if (mbar_try_wait(bar, parity, suspend_ns)) return true;
     const uint64_t start = global_ns();
     for (uint32_t spin = 0;; ++spin) {
         if (mbar_try_wait(bar, parity, suspend_ns)) return true;
         if ((spin & 63) == 0) {
             if (*abort_flag) return false;
-            if (global_ns() - start > kWaitLimitNs) {
+            if (global_ns() - start > limit_ns) {
                 *abort_flag = 1;
                 atomicExch(status, kStatusWaitTimeout);
                 return false;
@@ -189,6 +224,19 @@ __device__ __forceinline__ bool mbar_wait_own(uint64_t* bar, uint32_t parity, ui
             return false;
         }
     }
+}
+
+// Named barrier `id` over `threads` threads that also returns whether `pred`
+// holds in every one of them: a group of warps takes one decision together,
+// so none of them is left waiting at a later barrier for a thread that left.
+__device__ __forceinline__ bool named_sync_all(uint32_t id, uint32_t threads, bool pred) {
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\t"
+                 "setp.ne.u32 p, %1, 0;\n\t"
+                 "bar.red.and.pred q, %2, %3, p;\n\t"
+                 "selp.u32 %0, 1, 0, q;\n\t}"
+                 : "=r"(r) : "r"(pred ? 1u : 0u), "r"(id), "r"(threads) : "memory");
+    return r != 0;
 }
 
 // ------------------------------------------------------- bulk async copy --

@@ -112,14 +112,17 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
                 for (uint32_t jj = 0; jj < nj; ++jj)
                     bulk_load(stageT(s) + jj * kRows, terms + size_t(j0 + jj) * N + row0, rows * 4, &ctl->bfull[s]);
             };
-            for (uint32_t kc = 0; kc < kStages && kc < nkc; ++kc) load(kc);
+            uint32_t loaded = 0;                       // chunks 0..loaded-1 were copied
+            for (; loaded < kStages && loaded < nkc; ++loaded) load(loaded);
             const uint32_t idesc = idesc_f16_f32(kTileRows, NC);
             bool ok = true;
+            uint32_t used = 0;                         // chunks whose bfull this thread saw complete
             for (uint32_t kc = 0; ok && kc < nkc; ++kc) {
                 const uint32_t s = kc % kStages, sp = (kc / kStages) & 1;
-                ok = mbar_wait(&ctl->afull[s], sp, abort_flag, a.status);
-                if (ok) ok = mbar_wait(&ctl->bfull[s], sp, abort_flag, a.status);
+                ok = mbar_wait(&ctl->afull[s], sp, abort_flag, a.status, a.wait_limit_ns);
+                if (ok) ok = mbar_wait(&ctl->bfull[s], sp, abort_flag, a.status, a.wait_limit_ns);
                 if (!ok) break;
+                used = kc + 1;
                 tc_fence_after();
                 const uint32_t kl = chunk_k(a.k_total, kc);
                 const uint32_t sbo = (kl / 8) * 128;
@@ -134,12 +137,17 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
                 if (kc >= 1 && kc - 1 + kStages < nkc) {
                     // Chunk kc-1's MMAs retired: its stage (A, B and t_j) takes chunk kc-1+kStages.
                     const uint32_t pc = kc - 1;
-                    ok = mbar_wait(&ctl->sempty[pc % kStages], (pc / kStages) & 1, abort_flag, a.status);
-                    if (ok) load(pc + kStages);
+                    ok = mbar_wait(&ctl->sempty[pc % kStages], (pc / kStages) & 1, abort_flag, a.status, a.wait_limit_ns);
+                    if (ok) load(loaded++);
                 }
             }
+            // This thread's own work must finish before the CTA leaves: the
+            // copies of chunks it never consumed (distinct stages), then every
+            // MMA it issued (accfull completes when they have all retired).
+            for (uint32_t c = used; c < loaded; ++c)
+                mbar_wait_own(&ctl->bfull[c % kStages], (c / kStages) & 1, a.status);
             mma_commit(&ctl->accfull);
-            mbar_wait(&ctl->accfull, 0, abort_flag, a.status);
+            mbar_wait_own(&ctl->accfull, 0, a.status);
         }
         __syncwarp();
     } else {
@@ -152,7 +160,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
         for (uint32_t kc = 0; ok && kc < nkc; ++kc) {
             const uint32_t s = kc % kStages;
             // bfull(kc) also implies chunk kc-kStages retired, so the A stage is free.
-            ok = mbar_wait(&ctl->bfull[s], (kc / kStages) & 1, abort_flag, a.status);
+            ok = mbar_wait(&ctl->bfull[s], (kc / kStages) & 1, abort_flag, a.status, a.wait_limit_ns);
             if (!ok) break;
             const uint32_t kl = chunk_k(a.k_total, kc);
             uint8_t* tileA = stageA(s) + tile * kTileRows * kl * 2;
@@ -189,7 +197,8 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
         }
 
         // ---- epilogue.
-        if (ok) ok = mbar_wait(&ctl->accfull, 0, abort_flag, a.status);
+        if (ok) ok = mbar_wait(&ctl->accfull, 0, abort_flag, a.status, a.wait_limit_ns);
+        ok = __all_sync(0xffffffffu, ok);                   // the TMEM loads are warp-collective
         const uint32_t st = L | 1u;                        // odd staging stride
         if (ok) {
             tc_fence_after();

@@ -143,7 +143,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                                         (a.terms_tiled ? size_t(row0) * P : size_t(row0));
                 for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
                     const uint32_t s = g % kPStages;
-                    if (g >= kPStages && !mbar_wait(&ctl->sempty[s], ((g / kPStages) - 1) & 1, abort_flag, a.status, kSuspendNs)) {
+                    if (g >= kPStages && !mbar_wait(&ctl->sempty[s], ((g / kPStages) - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
                         ok = false;
                         break;
                     }
@@ -174,14 +174,14 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             uint32_t g = 0, it = 0;
             for (uint32_t job = blockIdx.x; ok && job < njobs; job += gridDim.x, ++it) {
                 const uint32_t buf = it & 1;
-                if (it >= 2 && !mbar_wait(&ctl->accempty[buf], ((it / 2) - 1) & 1, abort_flag, a.status, kSuspendNs)) {
+                if (it >= 2 && !mbar_wait(&ctl->accempty[buf], ((it / 2) - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
                     const uint32_t s = g % kPStages;
-                    if (!mbar_wait(&ctl->afull[s], (g / kPStages) & 1, abort_flag, a.status, kSuspendNs)) {
+                    if (!mbar_wait(&ctl->afull[s], (g / kPStages) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
                         ok = false;
                         break;
                     }
@@ -230,7 +230,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                 }
                 if (!mine) continue;
                 const uint32_t s = g % kPStages;
-                if (ok) ok = mbar_wait(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status, kSuspendNs);
+                if (ok) ok = mbar_wait(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs);
                 const uint32_t kl = chunk_k(a.k_total, kc);
                 const uint32_t* ts = stageT(s) + row;
                 uint32_t t[kTermsPerChunk];
@@ -287,7 +287,10 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             const uint32_t prod = job / ntiles, row0 = (job % ntiles) * kTileRows;
             const uint32_t rows = min(kTileRows, N - row0);
             const bool valid = row < rows;
-            if (ok) ok = mbar_wait(&ctl->accfull[buf], (it / 2) & 1, abort_flag, a.status, kSuspendNs);
+            if (ok) ok = mbar_wait(&ctl->accfull[buf], (it / 2) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs);
+            // The TMEM loads are warp-collective: a warp reads its lanes only if
+            // every thread of it saw the accumulator complete.
+            ok = __all_sync(0xffffffffu, ok);
             uint32_t z[LT ? LT : 1];
             int64_t top = 0;
             if (ok) {

@@ -149,15 +149,17 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             const uint32_t bbytes = gcols * K * 2;
             mbar_arrive_expect_tx(&ctl->bfull, bbytes);
             bulk_load(bres, a.enc_b + size_t(col0) * K, bbytes, &ctl->bfull);
-            bool ok = mbar_wait(&ctl->bfull, 0, abort_flag, a.status, kCtlSuspendNs);
+            // This thread's own copy: it must land before the CTA can leave.
+            bool ok = mbar_wait_own(&ctl->bfull, 0, a.status, kCtlSuspendNs);
             const uint32_t sbo = (K / 8) * 128;
             const uint32_t idesc = idesc_f16_f32(kTileRows, gcols);
             const uint32_t b_addr = smem_u32(bres);
             uint32_t ii = 0;
             for (uint32_t job = slot; ok && job < njobs; job += nslots, ++ii) {
                 const uint32_t s = ii & 1, use = ii >> 1;
-                ok = mbar_wait(&ctl->afull[s], use & 1, abort_flag, a.status, kCtlSuspendNs);
-                if (ok && ii >= 2) ok = mbar_wait(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status, kCtlSuspendNs);
+                ok = mbar_wait(&ctl->afull[s], use & 1, abort_flag, a.status, a.wait_limit_ns, kCtlSuspendNs);
+                if (ok && ii >= 2)
+                    ok = mbar_wait(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kCtlSuspendNs);
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t a_addr = smem_u32(tiles + s * tile_bytes);
@@ -167,10 +169,10 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
                 mma_commit(&ctl->accfull[s]);
                 mma_commit(&ctl->aempty[s]);
             }
-            // Drain the last commits before TMEM is freed.
+            // This thread's own MMAs (ii jobs issued) retire before TMEM is freed.
             for (uint32_t back = 1; back <= 2 && back <= ii; ++back) {
                 const uint32_t jj = ii - back;
-                mbar_wait(&ctl->aempty[jj & 1], (jj >> 1) & 1, abort_flag, a.status, kCtlSuspendNs);
+                mbar_wait_own(&ctl->aempty[jj & 1], (jj >> 1) & 1, a.status, kCtlSuspendNs);
             }
         }
         __syncwarp();
@@ -182,10 +184,17 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
         const uint32_t grp = warp / kBuildGroupWarps;           // = the A buffer this group fills
         const uint32_t r = threadIdx.x - grp * kBuildGroupWarps * 32;
         const uint32_t stage_off = (tile_bytes - kTileRows * L * 4) & ~15u;
+        const uint32_t bar_id = 1 + grp;                        // named barriers 1 and 2
+        const uint32_t vote_id = 3 + grp;                       // 3 and 4: the group's joint decision
         uint32_t ii = grp;
         for (uint32_t job = slot + grp * nslots; job < njobs; job += 2 * nslots, ii += 2) {
             const uint32_t s = ii & 1, use = ii >> 1;
-            if (ii >= 2 && !mbar_wait(&ctl->aempty[s], (use - 1) & 1, abort_flag, a.status)) break;
+            // The MMA has released this buffer.  The group leaves together or
+            // not at all: a thread that gave up alone would strand the others
+            // at the group's named barrier below.
+            const bool free_ok = ii < 2 || mbar_wait(&ctl->aempty[s], (use - 1) & 1, abort_flag, a.status,
+                                                     a.wait_limit_ns);
+            if (!named_sync_all(vote_id, kBuildGroupWarps * 32, free_ok)) break;
             const uint32_t tile = job % ntiles, operand = (job / ntiles) % a.operands;
             const uint32_t prod = job / (ntiles * a.operands);
             const uint32_t rows = min(kTileRows, a.N - tile * kTileRows);
@@ -207,17 +216,17 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
                           bytes, &ctl->infull[s]);
             }
             const bool valid = r < rows;
-            const bool ok_in = mbar_wait(&ctl->infull[s], use & 1, abort_flag, a.status);
+            // The group's own copy: every builder waits for it to land (never
+            // cut short by the abort flag, so no copy is left in flight).
+            const bool ok_in = mbar_wait_own(&ctl->infull[s], use & 1, a.status);
             uint32_t w[LT ? LT : 64];
 #pragma unroll
             for (uint32_t l = 0; l < (LT ? uint32_t(LT) : 64u); ++l) {
                 if (!LT && l >= L) break;
                 w[l] = (valid && ok_in) ? staged[r * L + l] : 0u;
             }
-            // One named barrier per builder group (ids 1 and 2).
-            if (grp == 0) asm volatile("bar.sync 1, %0;" :: "r"(kBuildGroupWarps * 32) : "memory");
-            else asm volatile("bar.sync 2, %0;" :: "r"(kBuildGroupWarps * 32) : "memory");
-            if (!ok_in) break;
+            // Every row is read before any digit is written over the staging.
+            asm volatile("bar.sync %0, %1;" :: "r"(bar_id), "r"(kBuildGroupWarps * 32) : "memory");
             if (valid) {
                 digits_row<LT>(buf, r, w, L, K);
             } else {
@@ -228,9 +237,9 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             mbar_arrive(&ctl->afull[s]);
         }
     } else {
-        // ---- epilogue: quarter of TMEM lanes, a third of the group's primes.
+        // ---- epilogue: quarter of TMEM lanes, a quarter of the group's primes.
         const uint32_t e = warp - kBuildWarps;
-        const uint32_t quarter = e & 3, part = e >> 2;        // part 0..2
+        const uint32_t quarter = e & 3, part = e >> 2;        // part 0..kEpiPerQuarter-1
         const uint32_t r = quarter * 32 + lane;
         const uint32_t gp = gcols / 4;                        // primes in this group (incl. padding)
         const uint32_t per = (gp + kEpiPerQuarter - 1) / kEpiPerQuarter;
@@ -238,7 +247,9 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
         uint32_t ii = 0;
         for (uint32_t job = slot; job < njobs; job += nslots, ++ii) {
             const uint32_t s = ii & 1, use = ii >> 1;
-            if (!mbar_wait(&ctl->accfull[s], use & 1, abort_flag, a.status)) break;
+            const bool ok = mbar_wait(&ctl->accfull[s], use & 1, abort_flag, a.status, a.wait_limit_ns);
+            // The TMEM loads below are warp-collective: the warp leaves as one.
+            if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
             const uint32_t tile = job % ntiles, operand = (job / ntiles) % a.operands;
             const uint32_t prod = job / (ntiles * a.operands);
@@ -246,9 +257,10 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             const bool valid = i < a.N;
             uint32_t* planes = (operand ? a.out1 : a.out0) + size_t(prod) * a.out_stride;
             const uint32_t taddr = tmem + ((quarter * 32) << 16) + s * 256;
-            // Up to 24 primes (96 columns) per warp, 32 columns (8 primes) at a time.
+            // Up to 60 primes per group (240 columns): at most 15 primes (60
+            // columns) per warp, read 32 columns (8 primes) at a time.
 #pragma unroll 1
-            for (uint32_t cb = 0; cb < 3; ++cb) {
+            for (uint32_t cb = 0; cb < 2; ++cb) {
                 if (cb * 8 >= p1 - p0) break;                       // warp-uniform
                 float v[32];
                 tmem_ld32(taddr + 4 * p0 + cb * 32, v);

@@ -86,6 +86,7 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
         enc_.prime[j] = make_uint2(plan_.prime_consts[4 * j], plan_.prime_consts[4 * j + 1]);
     enc_.N = g.N; enc_.L = g.L; enc_.P = g.P; enc_.K = g.enc_k; enc_.cols = g.enc_cols; enc_.chunks = g.enc_chunks;
     enc_.status = status_.as<uint32_t>();
+    enc_.wait_limit_ns = kWaitLimitNs;
 
     crt_.crt_b = crt_b_.as<uint16_t>();
     for (uint32_t j = 0; j < g.P; ++j) crt_.invp[j] = plan_.invp[j];
@@ -96,6 +97,7 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     crt_.gap = plan_.gap;
     crt_.top_bits = g.W - 32 * (g.L - 1);
     crt_.status = status_.as<uint32_t>();
+    crt_.wait_limit_ns = kWaitLimitNs;
 
     // Products per launch chain: long chains amortise each kernel's launch and
     // tail (8 products per chain at N=65536 measured 16% faster than 1).
@@ -151,6 +153,10 @@ void Context::set_row_bits(uint32_t row_bits) {
 }
 
 void Context::set_group(uint32_t g) { group_ = std::max<uint32_t>(1, g); }
+
+void Context::set_wait_limit_ns(uint64_t ns) {
+    enc_.wait_limit_ns = crt_.wait_limit_ns = ns ? ns : kWaitLimitNs;
+}
 
 uint32_t Context::host_group() const {
     // Host-buffer calls pipeline copies against compute in chunks of about
@@ -504,7 +510,7 @@ void Context::check_status() {
     check(cudaMemcpy(&st, status_.ptr, 4, cudaMemcpyDeviceToHost), "status read");
     if (st != kStatusOk) {
         check(cudaMemset(status_.ptr, 0, 4), "status reset");
-        throw DeviceTimeout("a kernel's bounded wait ran out (device status " + std::to_string(st) + ")");
+        raise_device_status(st);
     }
 }
 

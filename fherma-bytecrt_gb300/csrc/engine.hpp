@@ -42,6 +42,13 @@ inline void check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw CudaError(what, e);
 }
 
+// The device status word a context's kernels write (common.cuh DeviceStatus)
+// as the host reports it: any value but kStatusOk is a wait that ran out.
+inline void raise_device_status(uint32_t st) {
+    if (st != 0)
+        throw DeviceTimeout("a kernel's bounded wait ran out (device status " + std::to_string(st) + ")");
+}
+
 struct DeviceBuffer {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -147,6 +154,11 @@ public:
     NttArgs ntt_args() const { return ntt_; }
     const Tuning& tuning() const { return tuning_; }
     void set_tuning(const Tuning& t);
+    // Limit of the kernels' waits on another role's arrival (0: the default,
+    // kWaitLimitNs).  A wait that runs out makes the call report
+    // DeviceTimeout; waits on a thread's own copies and MMAs keep kWaitLimitNs.
+    void set_wait_limit_ns(uint64_t ns);
+    uint64_t wait_limit_ns() const { return enc_.wait_limit_ns; }
     // NTT split N = C * 2^row_bits (0: the default R = min(N, 256)); re-plans the NTT tables.
     void set_row_bits(uint32_t row_bits);
 

@@ -24,6 +24,7 @@ struct EncodeArgs {
     const uint16_t* enc_b;   // fp16 byte-power matrix, chunked
     uint32_t N, L, P, K, cols, chunks;
     uint32_t* status;
+    uint64_t wait_limit_ns;  // limit of waits on other roles (the context's wait limit)
     uint32_t groups, group_cols, nprod, operands;   // set by the launcher
     uint2 prime[kMaxPrimes]; // p, p^-1 mod 2^32
 };
@@ -37,6 +38,7 @@ struct CrtArgs {
     double q_inv_scaled;
     uint32_t N, L, P, k_total, kchunks, E, NC;
     uint32_t* status;
+    uint64_t wait_limit_ns;  // limit of waits on other roles (the context's wait limit)
     uint32_t q[kMaxLimbs];
     float invp[256];         // float(1/p_j): warp-uniform reads from the constant cache
     uint32_t terms_tiled;    // persistent CRT only: terms tile-major, [N/128][P][128]

@@ -94,7 +94,19 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *                3 (8) or 4 (16, R = 256 only)
  *   "row_rows"   rows per row-pass CTA; 0: up to 128 with 16 elements per thread, else 32
  *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
- *                Re-plans the twiddle and twist tables (the primes stay). */
+ *                Re-plans the twiddle and twist tables (the primes stay).
+ *   "wait_limit_ns"  limit of a kernel's wait on another warp role's arrival,
+ *                in ns (0: the default, 2 s).  A lower bound: a wait reads the
+ *                clock every 64 polls and a poll may sleep up to 20 us, so it
+ *                can overrun by about a millisecond.  Under 1000 (finer than
+ *                the device clock resolves) a wait gives up at once if the
+ *                arrival is missing.  A wait that runs out makes the
+ *                kernel skip its remaining work, drain its own copies and MMAs
+ *                and return; the call then reports BCG_ERR_DEVICE_TIMEOUT and
+ *                the context stays usable.  Waits on a thread's own copies and
+ *                MMAs always keep 2 s.  The reference reports CUDA failures
+ *                through check() (native-smoke/solve.cu:46-49); it has no
+ *                bounded device waits. */
 int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value);
 int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* value);
 /* Autotuner: times whole launch chains on synthetic operands for every value
@@ -138,7 +150,8 @@ int bcg_multiply_device(bcg_context* ctx, const uint32_t* a, const uint32_t* b, 
  * loads it.  A product needs 2*P*N words of it, so points up to N=32768 with
  * W around 868 bits fit; larger points return BCG_ERR_INVALID.  The first call
  * on a device looks up the array's device address (make it before any stream
- * capture).  Calls that overlap on the GPU race on the shared array. */
+ * capture; the address is kept, so do not use this entry point across a
+ * cudaDeviceReset).  Calls that overlap on the GPU race on the shared array. */
 int bcg_multiply_device_static(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c,
                                uint32_t count, void* stream);
 
