@@ -16,13 +16,16 @@
 // Set-up: host code cannot use the array's name as a device address, so the
 // first call on each device looks up the address with cudaGetSymbolAddress,
 // with that device current, and keeps it.  Make that first call before any
-// stream capture.  All calls share the array: calls that overlap on the GPU
-// (different streams, contexts or threads) race on it.  Nothing in it needs
-// to start at zero; every word a call reads was written earlier by the same
-// call.
+// stream capture.  The address stays valid for the life of the device's
+// primary context: after cudaDeviceReset the library's module is loaded
+// again elsewhere, so do not call this entry point across a device reset.
+// All calls share the array: calls that overlap on the GPU (different
+// streams, contexts or threads) race on it.  Nothing in it needs to start at
+// zero; every word a call reads was written earlier by the same call.
 #include "../../include/bytecrt_gb300.h"
 #include "capi_internal.hpp"
 
+#include <algorithm>
 #include <mutex>
 
 namespace {
@@ -69,7 +72,12 @@ extern "C" int bcg_multiply_device_static(bcg_context* ctx, const uint32_t* a, c
                                         std::to_string(kStaticScratchWords));
         uint32_t* ws = scratch_address(x.device());
         cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : x.stream();
-        const uint32_t fit = uint32_t(kStaticScratchWords / per_product);
+        // Products per launch chain: as many as the scratch holds, but no more
+        // than the context's own chain length (the allocating path's group),
+        // which keeps every stage's grid within its limits (the column pass
+        // puts 2 x products on grid.z).
+        const uint32_t fit = uint32_t(std::min<size_t>(kStaticScratchWords / per_product,
+                                                       std::max<uint32_t>(1u, x.group())));
         const size_t cw = x.coeff_words();
         const bcg::NttArgs ntt = x.ntt_args();
         for (uint32_t done = 0; done < count; done += fit) {
