@@ -105,7 +105,7 @@ def test_multiply_device_matches_oracle(N, W):
 @pytest.mark.parametrize("kind_a,kind_b", [("zero", "random"), ("one", "random"), ("minus_one", "minus_one"),
                                            ("half_low", "half_high"), ("half_high", "half_high"),
                                            ("minus_one", "one")])
-@pytest.mark.parametrize("N,W", [(1024, 868), (32768, 868)])
+@pytest.mark.parametrize("N,W", [(1024, 868), (32768, 868), (65536, 1747)])
 def test_edge_fixtures(N, W, kind_a, kind_b):
     pkg = package()
     m, o, q = setup(N, W, 5)

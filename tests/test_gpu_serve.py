@@ -123,3 +123,50 @@ def test_close_finishes_pending_requests():
     want = alone(pkg, N, W, q, a, b)
     for c in outs:
         assert np.array_equal(c, want)
+
+
+def test_config5_geometries_identical_alone_and_in_the_mix():
+    """The served workload's three points (N=16384/W=434, 32768/868,
+    65536/1747), about 30 mixed requests from two threads, half of them with a
+    resident left operand: every response equals the same product run alone,
+    and one response per geometry equals the oracle's product."""
+    pkg = package()
+    rng = np.random.default_rng(55)
+    srv = pkg.Server(slots=3)
+    pts = []
+    for k, (N, W) in enumerate(((16384, 434), (32768, 868), (65536, 1747))):
+        q = pkg.inputs.modulus(W, 60 + k)
+        pid = srv.add_point(N, W, q)
+        a_res = pkg.inputs.uniform(q, N, 600 + k)
+        oid = srv.add_operand(pid, a_res)
+        pts.append(dict(N=N, W=W, q=q, pid=pid, a_res=a_res, oid=oid, m=pkg.Multiplier(N, W, q)))
+    reqs = []
+    for i in range(30):
+        p = pts[i % 3] if i < 3 else pts[int(rng.integers(3))]
+        resident = bool(i % 2)
+        a = p["a_res"] if resident else pkg.inputs.uniform(p["q"], p["N"], 7000 + i)
+        b = pkg.inputs.uniform(p["q"], p["N"], 8000 + i)
+        reqs.append(dict(p=p, a=a, b=b, c=np.zeros_like(b), oid=p["oid"] if resident else 0))
+    ids = [None] * len(reqs)
+
+    def submit(part):
+        for i in part:
+            r = reqs[i]
+            ids[i] = srv.submit(r["p"]["pid"], r["b"], r["c"], a=None if r["oid"] else r["a"], operand=r["oid"])
+
+    threads = [threading.Thread(target=submit, args=(range(k, len(reqs), 2),)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for i in ids:
+        srv.wait(i)
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    for r in reqs:
+        assert np.array_equal(r["c"], r["p"]["m"].multiply(r["a"], r["b"])), (r["p"]["N"], bool(r["oid"]))
+    for p in pts:
+        r = next(r for r in reqs if r["p"] is p)
+        assert np.array_equal(r["c"], O.Oracle(p["N"], p["W"], p["q"]).multiply(r["a"], r["b"])), p["N"]
+        p["m"].close()
+    srv.close()
