@@ -43,7 +43,7 @@ class _State:
         q = np.ascontiguousarray(p.q, dtype=np.uint32).reshape(-1)
         if q.shape[0] != p.L:
             raise RuntimeError("modulus limb count")
-        if p.B > 128 or (p.B == 0 and False):
+        if p.B > 128:
             raise RuntimeError("batch coverage B=1..128")
         self.point = p
         self.mult = Multiplier(p.N, p.W, q)

@@ -7,8 +7,9 @@
 #    with oracle/ref_kernels.cu into the device-only cubin
 #    oracle/_ref/ref_kernels.cubin for sm_103a (loaded by oracle/ref_kernels.py
 #    to time the reference's kernels on the GB300).
-# Runs only where the reference checkout exists.  Nothing of the reference is
-# copied into the repository.
+# Runs only where the reference checkout exists: REFERENCE_ROOT, else the
+# checkout's place in the build container (this recipe is the one file that
+# names it).  Nothing of the reference is copied into the repository.
 set -eu
 REF=${REFERENCE_ROOT:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)

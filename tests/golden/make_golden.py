@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Regenerate the committed golden vectors from the reference checkout.
 
-Runs only in a container that has the reference (default /root/reference,
-override with REFERENCE_ROOT).  It reads the reference's own artefacts and
+Runs only in a container that has the reference checkout, named by the
+REFERENCE_ROOT environment variable.  It reads the reference's own artefacts and
 writes compact fixtures under tests/golden/, which the tests then use on any
 machine (the reference itself does not travel):
 
@@ -32,7 +32,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("REFERENCE_ROOT", "")
+if not os.path.isdir(REF):
+    sys.exit("set REFERENCE_ROOT to the reference checkout")
 
 
 def words(v: int, n: int):
