@@ -65,6 +65,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
     CrtSmem* ctl = reinterpret_cast<CrtSmem*>(smem + kStages * stage_bytes);
     uint32_t* zbuf = reinterpret_cast<uint32_t*>(smem);          // epilogue staging (after all MMAs)
     volatile uint32_t* abort_flag = &ctl->abort_flag;
+    const WaitLimit wl = wait_limit(a.wait_limit_ns);   // read once: no parameter load ahead of a poll
     auto stageA = [&](uint32_t s) { return smem + s * stage_bytes; };
     auto stageB = [&](uint32_t s) { return smem + s * stage_bytes + a_bytes; };
     auto stageT = [&](uint32_t s) { return reinterpret_cast<uint32_t*>(smem + s * stage_bytes + a_bytes + b_bytes); };
@@ -119,8 +120,8 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
             uint32_t used = 0;                         // chunks whose bfull this thread saw complete
             for (uint32_t kc = 0; ok && kc < nkc; ++kc) {
                 const uint32_t s = kc % kStages, sp = (kc / kStages) & 1;
-                ok = mbar_wait(&ctl->afull[s], sp, abort_flag, a.status, a.wait_limit_ns);
-                if (ok) ok = mbar_wait(&ctl->bfull[s], sp, abort_flag, a.status, a.wait_limit_ns);
+                ok = mbar_wait(&ctl->afull[s], sp, abort_flag, a.status, wl);
+                if (ok) ok = mbar_wait(&ctl->bfull[s], sp, abort_flag, a.status, wl);
                 if (!ok) break;
                 used = kc + 1;
                 tc_fence_after();
@@ -137,7 +138,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
                 if (kc >= 1 && kc - 1 + kStages < nkc) {
                     // Chunk kc-1's MMAs retired: its stage (A, B and t_j) takes chunk kc-1+kStages.
                     const uint32_t pc = kc - 1;
-                    ok = mbar_wait(&ctl->sempty[pc % kStages], (pc / kStages) & 1, abort_flag, a.status, a.wait_limit_ns);
+                    ok = mbar_wait(&ctl->sempty[pc % kStages], (pc / kStages) & 1, abort_flag, a.status, wl);
                     if (ok) load(loaded++);
                 }
             }
@@ -160,7 +161,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
         for (uint32_t kc = 0; ok && kc < nkc; ++kc) {
             const uint32_t s = kc % kStages;
             // bfull(kc) also implies chunk kc-kStages retired, so the A stage is free.
-            ok = mbar_wait(&ctl->bfull[s], (kc / kStages) & 1, abort_flag, a.status, a.wait_limit_ns);
+            ok = mbar_wait(&ctl->bfull[s], (kc / kStages) & 1, abort_flag, a.status, wl);
             if (!ok) break;
             const uint32_t kl = chunk_k(a.k_total, kc);
             uint8_t* tileA = stageA(s) + tile * kTileRows * kl * 2;
@@ -197,7 +198,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
         }
 
         // ---- epilogue.
-        if (ok) ok = mbar_wait(&ctl->accfull, 0, abort_flag, a.status, a.wait_limit_ns);
+        if (ok) ok = mbar_wait(&ctl->accfull, 0, abort_flag, a.status, wl);
         ok = __all_sync(0xffffffffu, ok);                   // the TMEM loads are warp-collective
         const uint32_t st = L | 1u;                        // odd staging stride
         if (ok) {

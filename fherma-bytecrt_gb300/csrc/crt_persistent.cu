@@ -98,6 +98,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
     uint32_t* zstage = reinterpret_cast<uint32_t*>(smem + kPStages * stage_bytes);
     PSmem* ctl = reinterpret_cast<PSmem*>(smem + kPStages * stage_bytes + zstage_bytes_for(L));
     volatile uint32_t* abort_flag = &ctl->abort_flag;
+    const WaitLimit wl = wait_limit(a.wait_limit_ns);   // read once: no parameter load ahead of a poll
     auto stageA = [&](uint32_t s) { return smem + s * stage_bytes; };
     auto stageB = [&](uint32_t s) { return smem + s * stage_bytes + a_bytes; };
     auto stageT = [&](uint32_t s) { return reinterpret_cast<uint32_t*>(smem + s * stage_bytes + a_bytes + b_bytes); };
@@ -143,7 +144,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                                         (a.terms_tiled ? size_t(row0) * P : size_t(row0));
                 for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
                     const uint32_t s = g % kPStages;
-                    if (g >= kPStages && !mbar_wait(&ctl->sempty[s], ((g / kPStages) - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
+                    if (g >= kPStages && !mbar_wait(&ctl->sempty[s], ((g / kPStages) - 1) & 1, abort_flag, a.status, wl, kSuspendNs)) {
                         ok = false;
                         break;
                     }
@@ -174,14 +175,14 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             uint32_t g = 0, it = 0;
             for (uint32_t job = blockIdx.x; ok && job < njobs; job += gridDim.x, ++it) {
                 const uint32_t buf = it & 1;
-                if (it >= 2 && !mbar_wait(&ctl->accempty[buf], ((it / 2) - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
+                if (it >= 2 && !mbar_wait(&ctl->accempty[buf], ((it / 2) - 1) & 1, abort_flag, a.status, wl, kSuspendNs)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
                     const uint32_t s = g % kPStages;
-                    if (!mbar_wait(&ctl->afull[s], (g / kPStages) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
+                    if (!mbar_wait(&ctl->afull[s], (g / kPStages) & 1, abort_flag, a.status, wl, kSuspendNs)) {
                         ok = false;
                         break;
                     }
@@ -230,7 +231,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                 }
                 if (!mine) continue;
                 const uint32_t s = g % kPStages;
-                if (ok) ok = mbar_wait(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs);
+                if (ok) ok = mbar_wait(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status, wl, kSuspendNs);
                 const uint32_t kl = chunk_k(a.k_total, kc);
                 const uint32_t* ts = stageT(s) + row;
                 uint32_t t[kTermsPerChunk];
@@ -287,7 +288,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             const uint32_t prod = job / ntiles, row0 = (job % ntiles) * kTileRows;
             const uint32_t rows = min(kTileRows, N - row0);
             const bool valid = row < rows;
-            if (ok) ok = mbar_wait(&ctl->accfull[buf], (it / 2) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs);
+            if (ok) ok = mbar_wait(&ctl->accfull[buf], (it / 2) & 1, abort_flag, a.status, wl, kSuspendNs);
             // The TMEM loads are warp-collective: a warp reads its lanes only if
             // every thread of it saw the accumulator complete.
             ok = __all_sync(0xffffffffu, ok);

@@ -12,8 +12,8 @@
 //
 // The reference computes the same residues with u8 mma.sync byte dots and a
 // u64 Barrett (native-smoke/rns-encode-mma.cuh:15-52, 148-252).  Balanced
-// digits make the fp16 path exact; it replaces the int8 path, whose tensor
-// rate on GB300 is far below the fp16 rate.
+// digits make the fp16 path exact; it replaces the int8 path, which sm_103a
+// does not have (ptxas rejects tcgen05.mma .kind::i8 for this target).
 //
 // Persistent kernel.  The primes are split into NG groups (NG = 2 for P > 16)
 // so that one group's byte-power matrix stays resident in shared memory for
@@ -117,6 +117,7 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
     uint8_t* bres = smem + 2 * tile_bytes;                    // gcols x K fp16, resident
     EncodeSmem* ctl = reinterpret_cast<EncodeSmem*>(bres + a.group_cols * K * 2);
     volatile uint32_t* abort_flag = &ctl->abort_flag;
+    const WaitLimit wl = wait_limit(a.wait_limit_ns);   // read once: no parameter load ahead of a poll
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t ntiles = (a.N + kTileRows - 1) / kTileRows;
@@ -157,9 +158,9 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             uint32_t ii = 0;
             for (uint32_t job = slot; ok && job < njobs; job += nslots, ++ii) {
                 const uint32_t s = ii & 1, use = ii >> 1;
-                ok = mbar_wait(&ctl->afull[s], use & 1, abort_flag, a.status, a.wait_limit_ns, kCtlSuspendNs);
+                ok = mbar_wait(&ctl->afull[s], use & 1, abort_flag, a.status, wl, kCtlSuspendNs);
                 if (ok && ii >= 2)
-                    ok = mbar_wait(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kCtlSuspendNs);
+                    ok = mbar_wait(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status, wl, kCtlSuspendNs);
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t a_addr = smem_u32(tiles + s * tile_bytes);
@@ -193,7 +194,7 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             // not at all: a thread that gave up alone would strand the others
             // at the group's named barrier below.
             const bool free_ok = ii < 2 || mbar_wait(&ctl->aempty[s], (use - 1) & 1, abort_flag, a.status,
-                                                     a.wait_limit_ns);
+                                                     wl);
             if (!named_sync_all(vote_id, kBuildGroupWarps * 32, free_ok)) break;
             const uint32_t tile = job % ntiles, operand = (job / ntiles) % a.operands;
             const uint32_t prod = job / (ntiles * a.operands);
@@ -247,7 +248,7 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
         uint32_t ii = 0;
         for (uint32_t job = slot; job < njobs; job += nslots, ++ii) {
             const uint32_t s = ii & 1, use = ii >> 1;
-            const bool ok = mbar_wait(&ctl->accfull[s], use & 1, abort_flag, a.status, a.wait_limit_ns);
+            const bool ok = mbar_wait(&ctl->accfull[s], use & 1, abort_flag, a.status, wl);
             // The TMEM loads below are warp-collective: the warp leaves as one.
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
