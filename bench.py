@@ -31,6 +31,7 @@ import argparse
 import importlib
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -260,6 +261,39 @@ def rooflines(info, stage_us, sm_count, sm_mhz):
     return out
 
 
+def host_cpu() -> dict:
+    """The host cores a CPU leg runs on: model, logical CPUs, the affinity mask
+    and the physical cores in it (Linux /proc and /sys)."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if model is None:
+        try:   # Arm: the SoC name, else the implementer/part codes
+            with open("/sys/devices/soc0/machine") as f:
+                model = f.read().strip()
+        except OSError:
+            model = platform.processor() or platform.machine()
+    mask = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else list(range(os.cpu_count() or 1))
+    cores = set()
+    for cpu in mask:
+        base = f"/sys/devices/system/cpu/cpu{cpu}/topology/"
+        try:
+            with open(base + "core_id") as f1, open(base + "physical_package_id") as f2:
+                cores.add((f2.read().strip(), f1.read().strip()))
+        except OSError:
+            cores.add(("?", str(cpu)))
+    span = f"{mask[0]}-{mask[-1]}" if mask and mask == list(range(mask[0], mask[-1] + 1)) else ",".join(map(str, mask))
+    return {"model": model, "nproc": os.cpu_count(), "affinity": span, "physical_cores_in_mask": len(cores),
+            "arch": platform.machine()}
+
+
 def cpu_baseline(pkg, q, a, b, sample: int):
     from oracle import oracle
     o = oracle.Oracle(N, W, q)
@@ -268,7 +302,10 @@ def cpu_baseline(pkg, q, a, b, sample: int):
     for i in range(sample):
         o.multiply(a[i % a.shape[0]], b[i % b.shape[0]])
     dt = time.perf_counter() - t0
-    return {"value": sample / dt, "unit": "products/s", "cores": oracle.max_threads(), "kind": "port",
+    cpu = host_cpu()
+    threads = oracle.max_threads()
+    return {"value": sample / dt, "unit": "products/s", "cores": min(threads, cpu["physical_cores_in_mask"]),
+            "threads": threads, "kind": "port", "host": cpu,
             "sample": f"{sample} products of N=65536/W=1747 (oracle RNS-NTT-CRT restatement, OpenMP)"}
 
 
@@ -299,8 +336,12 @@ def run_reference(args):
         "config": {"workload": "N=65536 W=1747 L=55 P=114 exact negacyclic product, CPU, "
                                f"{per_step} product per step (bounded sample of the B=128 batch)",
                    "global_batch": per_step},
-        "cpu_baseline": {"value": value, "unit": "products/s", "cores": oracle.max_threads(), "kind": "port",
-                         "sample": f"{per_step} product per step, {args.steps} steps"},
+        "cpu_baseline": {"value": value, "unit": "products/s",
+                         "cores": min(oracle.max_threads(), host_cpu()["physical_cores_in_mask"]),
+                         "threads": oracle.max_threads(), "kind": "port", "host": host_cpu(),
+                         "sample": f"{per_step} product per step, {args.steps} steps",
+                         "reference_py": "not timed here: the reference checkout (reference.py) is not on this "
+                                         "machine; it checks the CRT only and has no product path"},
         "e2e": {"value": value, "unit": "products/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     line["gpu_kernels"] = reference_gpu_kernels()
@@ -508,7 +549,8 @@ def run_native(args):
         "config": {"workload": "batched B=128 exact negacyclic products, N=65536 W=1747 L=55 P=114, one q, "
                                "one CUDA graph per step",
                    "global_batch": B * world, "per_gpu_batch": B, "group": group, "graph_lanes": args.lanes,
-                   "tuning": {k: m.get_tuning(k) for k in ("crt_tiles", "crt_persistent", "row_local", "row_rows", "row_bits")},
+                   "tuning": {k: m.get_tuning(k) for k in ("crt_tiles", "crt_persistent", "row_local", "row_rows", "row_bits",
+                                                           "row_pass")},
                    "autotune": tuning,
                    "l2": "inputs larger than L2 (3.7 GB per step), no flush", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "products/s", "h2d_bytes_per_step": 2 * B * N * L * 4,
@@ -627,7 +669,8 @@ def autotune_geometries(pkg, args, device, geometries):
     for n, w in geometries:
         m = pkg.Multiplier(n, w, pkg.inputs.modulus(w, 1), device=device)
         r = m.autotune(max_group=16)
-        out[f"{n}/{w}"] = {k: r[k] for k in ("group", "crt_tiles", "crt_persistent", "row_local", "row_rows", "row_bits", "us_per_product_tuned")}
+        out[f"{n}/{w}"] = {k: r[k] for k in ("group", "crt_tiles", "crt_persistent", "row_local", "row_rows", "row_bits",
+                                             "row_pass", "us_per_product_tuned")}
         m.close()
     return out
 

@@ -26,10 +26,10 @@ std::map<Key, AutotuneReport>& tuned() {
 }
 
 struct Settings {
-    uint32_t row_bits, crt_tiles, crt_persistent, row_rows, row_local, group;
+    uint32_t row_bits, crt_tiles, crt_persistent, row_rows, row_local, group, row_pass;
     bool operator==(const Settings& o) const {
         return row_bits == o.row_bits && crt_tiles == o.crt_tiles && crt_persistent == o.crt_persistent &&
-               row_rows == o.row_rows && row_local == o.row_local && group == o.group;
+               row_rows == o.row_rows && row_local == o.row_local && group == o.group && row_pass == o.row_pass;
     }
 };
 
@@ -40,6 +40,7 @@ void apply(Context& ctx, const Settings& s) {
     t.crt_persistent = s.crt_persistent;
     t.row_rows = s.row_rows;
     t.row_local = s.row_local;
+    t.row_pass = s.row_pass;
     ctx.set_tuning(t);
     ctx.set_group(s.group);
 }
@@ -55,7 +56,7 @@ bool cached_autotune(int device, uint32_t N, uint32_t W, uint32_t L, AutotuneRep
 }
 
 void apply_autotune(Context& ctx, const AutotuneReport& r) {
-    apply(ctx, Settings{r.row_bits, r.crt_tiles, r.crt_persistent, r.row_rows, r.row_local, r.group});
+    apply(ctx, Settings{r.row_bits, r.crt_tiles, r.crt_persistent, r.row_rows, r.row_local, r.group, r.row_pass});
 }
 
 AutotuneReport autotune(Context& ctx, uint32_t max_group) {
@@ -114,7 +115,7 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
 
     AutotuneReport r{};
     Settings cur{g0.r_bits, ctx.tuning().crt_tiles, ctx.tuning().crt_persistent, ctx.tuning().row_rows,
-                 ctx.tuning().row_local, std::min(ctx.group(), gmax)};
+                 ctx.tuning().row_local, std::min(ctx.group(), gmax), ctx.tuning().row_pass};
     double cur_us = measure(cur);
     r.us_per_product_default = cur_us;
     auto consider = [&](Settings s) {
@@ -127,7 +128,7 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
         }
         if (us < cur_us * 0.99) { cur = s; cur_us = us; }
     };
-    // Coordinate search: radix split, CRT tile shape, row-pass CTA, chain length.
+    // Coordinate search: radix split, CRT tile shape, row-pass kernel and CTA, chain length.
     const uint32_t nb = g0.n_bits;
     for (uint32_t rb = (nb > 8 ? nb - 8 : 4); rb <= std::min<uint32_t>(8, nb); ++rb) {
         Settings s = cur; s.row_bits = rb; consider(s);
@@ -135,6 +136,7 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
     for (uint32_t t : {2u, 1u}) { Settings s = cur; s.crt_persistent = 0; s.crt_tiles = t; consider(s); }
     { Settings s = cur; s.crt_persistent = 1; consider(s); }
     for (uint32_t rl : {0u, 3u}) { Settings s = cur; s.row_local = rl; consider(s); }
+    for (uint32_t rp : {0u, 1u}) { Settings s = cur; s.row_pass = rp; consider(s); }
     for (uint32_t rr : {0u, 8u, 16u, 64u, 128u}) { Settings s = cur; s.row_rows = rr; consider(s); }
     for (uint32_t gr : {1u, 2u, 4u, 8u, 16u, 32u}) {
         if (gr > gmax) break;
@@ -148,6 +150,7 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
     r.crt_persistent = cur.crt_persistent;
     r.row_rows = cur.row_rows;
     r.row_local = cur.row_local;
+    r.row_pass = cur.row_pass;
     r.group = cur.group;
     r.us_per_product_tuned = cur_us;
     r.candidates = candidates;

@@ -127,6 +127,11 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
             bcg::Tuning t = c.tuning();
             t.row_rows = uint32_t(value);
             c.set_tuning(t);
+        } else if (k == "row_pass") {
+            require(value == 0 || value == 1, "row_pass must be 0 or 1");
+            bcg::Tuning t = c.tuning();
+            t.row_pass = uint32_t(value);
+            c.set_tuning(t);
         } else if (k == "wait_limit_ns") {
             require(value >= 0 && value <= 60000000000ll, "wait_limit_ns must be in [0, 6e10]");
             c.set_wait_limit_ns(uint64_t(value));
@@ -148,6 +153,7 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         else if (k == "crt_persistent") *value = c.tuning().crt_persistent;
         else if (k == "crt_gap_fold") *value = c.tuning().crt_gap_fold;
         else if (k == "row_local") *value = c.tuning().row_local;
+        else if (k == "row_pass") *value = c.tuning().row_pass;
         else if (k == "gap") *value = c.plan().gap;
         else if (k == "wait_limit_ns") *value = int64_t(c.wait_limit_ns());
         else throw std::invalid_argument("unknown tuning knob: " + k);
@@ -163,6 +169,7 @@ int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_repo
         out->candidates = r.candidates;
         out->crt_persistent = r.crt_persistent;
         out->row_local = r.row_local;
+        out->row_pass = r.row_pass;
         out->us_per_product_default = r.us_per_product_default;
         out->us_per_product_tuned = r.us_per_product_tuned;
     });

@@ -173,47 +173,48 @@ __device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 
-// The limit of waits on other roles, read from the kernel arguments once per
-// thread: a parameter load ahead of every poll measured 18.4 -> 21.4 us per
-// product in the CRT, whose chunk hand-offs are latency bound.  A limit under
-// 1 us is finer than %globaltimer resolves: such waits make one non-blocking
-// test and give up if the phase is incomplete (quick); a blocking poll may
-// suspend the thread long enough to cover a short wait.
-struct WaitLimit {
-    uint64_t ns;
-    bool quick;
-};
-__device__ __forceinline__ WaitLimit wait_limit(uint64_t ns) { return WaitLimit{ns, ns < 1000ull}; }
-
 // Bounded wait for another role's arrival.  Returns false (and records the
-// timeout) if the phase with the given parity did not complete within the
-// limit, or if another thread of the CTA already gave up (abort flag in
+// timeout) if the phase with the given parity did not complete within
+// limit_ns, or if another thread of the CTA already gave up (abort flag in
 // shared memory).  Threads of one warp can see different outcomes (one sees
 // the phase complete, another the abort flag): vote before a warp-collective
-// step.  The clock is read every 64 polls and a poll may suspend the thread
-// (up to suspend_ns, or a time the hardware chooses), so a wait can overrun
-// its limit by that much: the limit is a lower bound.
+// step.  The first poll is the whole fast path: the limit is read only once
+// the phase is found incomplete (the CRT's chunk hand-offs are latency bound;
+// a parameter load, a non-blocking test or a flag test ahead of the first poll
+// measured 18.4 -> 20.0-21.4 us per product there).  The clock is then read
+// every 64 polls and a poll may suspend the thread (up to suspend_ns, or a time
+// the hardware chooses), so a wait can overrun its limit by that much: the
+// limit is a lower bound.
+//
+// QUICK (kernels launched with a limit under 1 us, finer than %globaltimer
+// resolves): one non-blocking test, and the wait gives up if the phase is
+// incomplete; a blocking poll may suspend the thread long enough to cover a
+// short wait.
+template <bool QUICK = false>
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
                                           volatile uint32_t* abort_flag,
-                                          uint32_t* status, const WaitLimit& lim, uint32_t suspend_ns = 0) {
-    if (!lim.quick) {
+                                          uint32_t* status, uint64_t limit_ns, uint32_t suspend_ns = 0) {
+    if constexpr (QUICK) {
+        if (mbar_test_wait(bar, parity)) return true;
+        if (*abort_flag) return false;
+    } else {
         if (mbar_try_wait(bar, parity, suspend_ns)) return true;
         const uint64_t start = global_ns();
         for (uint32_t spin = 0;; ++spin) {
             if (mbar_try_wait(bar, parity, suspend_ns)) return true;
             if ((spin & 63) == 0) {
                 if (*abort_flag) return false;
-                if (global_ns() - start > lim.ns) break;
+                if (global_ns() - start > limit_ns) break;
             }
         }
-    } else {
-        if (mbar_test_wait(bar, parity)) return true;
-        if (*abort_flag) return false;
     }
     *abort_flag = 1;
     atomicExch(status, kStatusWaitTimeout);
     return false;
 }
+
+// Kernels are instantiated for both wait forms; launches with a limit under 1 us use QUICK.
+inline bool quick_waits(uint64_t limit_ns) { return limit_ns < 1000ull; }
 
 // Waits for this thread's own asynchronous work (copies, MMAs) to land before
 // the CTA leaves: bounded by the same limit, but not cut short by the abort

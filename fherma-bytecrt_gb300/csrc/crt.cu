@@ -50,7 +50,7 @@ struct CrtSmem {
     uint32_t abort_flag;
 };
 
-template <int LT, int TILES>
+template <int LT, int TILES, bool QUICK>
 __global__ void __launch_bounds__(CrtShape<TILES>::kThreads, CrtShape<TILES>::kMinBlocks)
 crt_kernel(const __grid_constant__ CrtArgs a) {
     constexpr uint32_t kTiles = TILES;
@@ -65,7 +65,6 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
     CrtSmem* ctl = reinterpret_cast<CrtSmem*>(smem + kStages * stage_bytes);
     uint32_t* zbuf = reinterpret_cast<uint32_t*>(smem);          // epilogue staging (after all MMAs)
     volatile uint32_t* abort_flag = &ctl->abort_flag;
-    const WaitLimit wl = wait_limit(a.wait_limit_ns);   // read once: no parameter load ahead of a poll
     auto stageA = [&](uint32_t s) { return smem + s * stage_bytes; };
     auto stageB = [&](uint32_t s) { return smem + s * stage_bytes + a_bytes; };
     auto stageT = [&](uint32_t s) { return reinterpret_cast<uint32_t*>(smem + s * stage_bytes + a_bytes + b_bytes); };
@@ -120,8 +119,8 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
             uint32_t used = 0;                         // chunks whose bfull this thread saw complete
             for (uint32_t kc = 0; ok && kc < nkc; ++kc) {
                 const uint32_t s = kc % kStages, sp = (kc / kStages) & 1;
-                ok = mbar_wait(&ctl->afull[s], sp, abort_flag, a.status, wl);
-                if (ok) ok = mbar_wait(&ctl->bfull[s], sp, abort_flag, a.status, wl);
+                ok = mbar_wait<QUICK>(&ctl->afull[s], sp, abort_flag, a.status, a.wait_limit_ns);
+                if (ok) ok = mbar_wait<QUICK>(&ctl->bfull[s], sp, abort_flag, a.status, a.wait_limit_ns);
                 if (!ok) break;
                 used = kc + 1;
                 tc_fence_after();
@@ -138,7 +137,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
                 if (kc >= 1 && kc - 1 + kStages < nkc) {
                     // Chunk kc-1's MMAs retired: its stage (A, B and t_j) takes chunk kc-1+kStages.
                     const uint32_t pc = kc - 1;
-                    ok = mbar_wait(&ctl->sempty[pc % kStages], (pc / kStages) & 1, abort_flag, a.status, wl);
+                    ok = mbar_wait<QUICK>(&ctl->sempty[pc % kStages], (pc / kStages) & 1, abort_flag, a.status, a.wait_limit_ns);
                     if (ok) load(loaded++);
                 }
             }
@@ -161,7 +160,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
         for (uint32_t kc = 0; ok && kc < nkc; ++kc) {
             const uint32_t s = kc % kStages;
             // bfull(kc) also implies chunk kc-kStages retired, so the A stage is free.
-            ok = mbar_wait(&ctl->bfull[s], (kc / kStages) & 1, abort_flag, a.status, wl);
+            ok = mbar_wait<QUICK>(&ctl->bfull[s], (kc / kStages) & 1, abort_flag, a.status, a.wait_limit_ns);
             if (!ok) break;
             const uint32_t kl = chunk_k(a.k_total, kc);
             uint8_t* tileA = stageA(s) + tile * kTileRows * kl * 2;
@@ -198,7 +197,7 @@ crt_kernel(const __grid_constant__ CrtArgs a) {
         }
 
         // ---- epilogue.
-        if (ok) ok = mbar_wait(&ctl->accfull, 0, abort_flag, a.status, wl);
+        if (ok) ok = mbar_wait<QUICK>(&ctl->accfull, 0, abort_flag, a.status, a.wait_limit_ns);
         ok = __all_sync(0xffffffffu, ok);                   // the TMEM loads are warp-collective
         const uint32_t st = L | 1u;                        // odd staging stride
         if (ok) {
@@ -234,11 +233,12 @@ size_t crt_smem_bytes(uint32_t NC, uint32_t tiles) {
 template <int LT, int TILES>
 static cudaError_t launch_crt_t(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
     const size_t smem = crt_smem_bytes(a.NC, TILES);
-    cudaError_t e = cudaFuncSetAttribute(crt_kernel<LT, TILES>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    auto* kern = quick_waits(a.wait_limit_ns) ? crt_kernel<LT, TILES, true> : crt_kernel<LT, TILES, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     constexpr uint32_t rows = CrtShape<TILES>::kRows;
     const dim3 grid((a.N + rows - 1) / rows, nprod);
-    crt_kernel<LT, TILES><<<grid, CrtShape<TILES>::kThreads, smem, st>>>(a);
+    kern<<<grid, CrtShape<TILES>::kThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 

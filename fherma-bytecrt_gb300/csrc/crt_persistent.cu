@@ -85,7 +85,7 @@ __device__ __forceinline__ void named_sync(uint32_t id, uint32_t threads) {
     asm volatile("bar.sync %0, %1;" :: "r"(id), "r"(threads) : "memory");
 }
 
-template <int LT, int GAP, int kPStages>
+template <int LT, int GAP, int kPStages, bool QUICK>
 __global__ void __launch_bounds__(kPThreads, 1)
 crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -98,7 +98,6 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
     uint32_t* zstage = reinterpret_cast<uint32_t*>(smem + kPStages * stage_bytes);
     PSmem* ctl = reinterpret_cast<PSmem*>(smem + kPStages * stage_bytes + zstage_bytes_for(L));
     volatile uint32_t* abort_flag = &ctl->abort_flag;
-    const WaitLimit wl = wait_limit(a.wait_limit_ns);   // read once: no parameter load ahead of a poll
     auto stageA = [&](uint32_t s) { return smem + s * stage_bytes; };
     auto stageB = [&](uint32_t s) { return smem + s * stage_bytes + a_bytes; };
     auto stageT = [&](uint32_t s) { return reinterpret_cast<uint32_t*>(smem + s * stage_bytes + a_bytes + b_bytes); };
@@ -144,7 +143,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                                         (a.terms_tiled ? size_t(row0) * P : size_t(row0));
                 for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
                     const uint32_t s = g % kPStages;
-                    if (g >= kPStages && !mbar_wait(&ctl->sempty[s], ((g / kPStages) - 1) & 1, abort_flag, a.status, wl, kSuspendNs)) {
+                    if (g >= kPStages && !mbar_wait<QUICK>(&ctl->sempty[s], ((g / kPStages) - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
                         ok = false;
                         break;
                     }
@@ -175,14 +174,14 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             uint32_t g = 0, it = 0;
             for (uint32_t job = blockIdx.x; ok && job < njobs; job += gridDim.x, ++it) {
                 const uint32_t buf = it & 1;
-                if (it >= 2 && !mbar_wait(&ctl->accempty[buf], ((it / 2) - 1) & 1, abort_flag, a.status, wl, kSuspendNs)) {
+                if (it >= 2 && !mbar_wait<QUICK>(&ctl->accempty[buf], ((it / 2) - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 for (uint32_t kc = 0; kc < nkc; ++kc, ++g) {
                     const uint32_t s = g % kPStages;
-                    if (!mbar_wait(&ctl->afull[s], (g / kPStages) & 1, abort_flag, a.status, wl, kSuspendNs)) {
+                    if (!mbar_wait<QUICK>(&ctl->afull[s], (g / kPStages) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs)) {
                         ok = false;
                         break;
                     }
@@ -231,7 +230,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
                 }
                 if (!mine) continue;
                 const uint32_t s = g % kPStages;
-                if (ok) ok = mbar_wait(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status, wl, kSuspendNs);
+                if (ok) ok = mbar_wait<QUICK>(&ctl->bfull[s], (g / kPStages) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs);
                 const uint32_t kl = chunk_k(a.k_total, kc);
                 const uint32_t* ts = stageT(s) + row;
                 uint32_t t[kTermsPerChunk];
@@ -288,7 +287,7 @@ crt_persistent_kernel(const __grid_constant__ CrtArgs a, uint32_t nprod) {
             const uint32_t prod = job / ntiles, row0 = (job % ntiles) * kTileRows;
             const uint32_t rows = min(kTileRows, N - row0);
             const bool valid = row < rows;
-            if (ok) ok = mbar_wait(&ctl->accfull[buf], (it / 2) & 1, abort_flag, a.status, wl, kSuspendNs);
+            if (ok) ok = mbar_wait<QUICK>(&ctl->accfull[buf], (it / 2) & 1, abort_flag, a.status, a.wait_limit_ns, kSuspendNs);
             // The TMEM loads are warp-collective: a warp reads its lanes only if
             // every thread of it saw the accumulator complete.
             ok = __all_sync(0xffffffffu, ok);
@@ -345,12 +344,13 @@ int sm_count_of_current_device() {
 template <int LT, int GAP, int ST>
 cudaError_t launch_persistent_t(const CrtArgs& a, uint32_t nprod, cudaStream_t st) {
     const size_t smem = smem_bytes_for(a.NC, a.L, ST);
-    cudaError_t e = cudaFuncSetAttribute(crt_persistent_kernel<LT, GAP, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem));
+    auto* kern = quick_waits(a.wait_limit_ns) ? crt_persistent_kernel<LT, GAP, ST, true>
+                                              : crt_persistent_kernel<LT, GAP, ST, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     const uint32_t jobs = nprod * ((a.N + kTileRows - 1) / kTileRows);
     const uint32_t grid = std::min<uint32_t>(jobs, uint32_t(sm_count_of_current_device()));
-    crt_persistent_kernel<LT, GAP, ST><<<grid, kPThreads, smem, st>>>(a, nprod);
+    kern<<<grid, kPThreads, smem, st>>>(a, nprod);
     return cudaGetLastError();
 }
 

@@ -102,7 +102,7 @@ __device__ __forceinline__ uint32_t encode_residue(float s0, float s1, float s2,
     return min(t + pc.x, t + 2 * pc.x);
 }
 
-template <int LT>
+template <int LT, bool QUICK>
 __global__ void __launch_bounds__(kEncThreads, 1)
 encode_kernel(const __grid_constant__ EncodeArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -117,7 +117,6 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
     uint8_t* bres = smem + 2 * tile_bytes;                    // gcols x K fp16, resident
     EncodeSmem* ctl = reinterpret_cast<EncodeSmem*>(bres + a.group_cols * K * 2);
     volatile uint32_t* abort_flag = &ctl->abort_flag;
-    const WaitLimit wl = wait_limit(a.wait_limit_ns);   // read once: no parameter load ahead of a poll
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t ntiles = (a.N + kTileRows - 1) / kTileRows;
@@ -158,9 +157,9 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             uint32_t ii = 0;
             for (uint32_t job = slot; ok && job < njobs; job += nslots, ++ii) {
                 const uint32_t s = ii & 1, use = ii >> 1;
-                ok = mbar_wait(&ctl->afull[s], use & 1, abort_flag, a.status, wl, kCtlSuspendNs);
+                ok = mbar_wait<QUICK>(&ctl->afull[s], use & 1, abort_flag, a.status, a.wait_limit_ns, kCtlSuspendNs);
                 if (ok && ii >= 2)
-                    ok = mbar_wait(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status, wl, kCtlSuspendNs);
+                    ok = mbar_wait<QUICK>(&ctl->accempty[s], (use - 1) & 1, abort_flag, a.status, a.wait_limit_ns, kCtlSuspendNs);
                 if (!ok) break;
                 tc_fence_after();
                 const uint32_t a_addr = smem_u32(tiles + s * tile_bytes);
@@ -193,8 +192,8 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
             // The MMA has released this buffer.  The group leaves together or
             // not at all: a thread that gave up alone would strand the others
             // at the group's named barrier below.
-            const bool free_ok = ii < 2 || mbar_wait(&ctl->aempty[s], (use - 1) & 1, abort_flag, a.status,
-                                                     wl);
+            const bool free_ok = ii < 2 || mbar_wait<QUICK>(&ctl->aempty[s], (use - 1) & 1, abort_flag, a.status,
+                                                     a.wait_limit_ns);
             if (!named_sync_all(vote_id, kBuildGroupWarps * 32, free_ok)) break;
             const uint32_t tile = job % ntiles, operand = (job / ntiles) % a.operands;
             const uint32_t prod = job / (ntiles * a.operands);
@@ -248,7 +247,7 @@ encode_kernel(const __grid_constant__ EncodeArgs a) {
         uint32_t ii = 0;
         for (uint32_t job = slot; job < njobs; job += nslots, ++ii) {
             const uint32_t s = ii & 1, use = ii >> 1;
-            const bool ok = mbar_wait(&ctl->accfull[s], use & 1, abort_flag, a.status, wl);
+            const bool ok = mbar_wait<QUICK>(&ctl->accfull[s], use & 1, abort_flag, a.status, a.wait_limit_ns);
             // The TMEM loads below are warp-collective: the warp leaves as one.
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
@@ -324,14 +323,15 @@ static cudaError_t launch_encode_t(EncodeArgs a, uint32_t nprod, cudaStream_t st
     a.nprod = nprod;
     a.operands = operands;
     const size_t smem = encode_smem_bytes(a.K, a.group_cols);
-    cudaError_t e = cudaFuncSetAttribute(encode_kernel<LT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    auto* kern = quick_waits(a.wait_limit_ns) ? encode_kernel<LT, true> : encode_kernel<LT, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     const uint32_t ntiles = (a.N + kTileRows - 1) / kTileRows;
     const uint32_t jobs = nprod * operands * ntiles;
     uint32_t slots = uint32_t(sm_count()) / a.groups;
     if (slots < 1) slots = 1;
     if (slots > jobs) slots = jobs;
-    encode_kernel<LT><<<slots * a.groups, kEncThreads, smem, st>>>(a);
+    kern<<<slots * a.groups, kEncThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 

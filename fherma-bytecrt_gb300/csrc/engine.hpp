@@ -95,6 +95,8 @@ public:
     virtual void end(cudaStream_t st) = 0;
 };
 
+class HostWorker;
+
 class Context {
 public:
     Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int device);
@@ -185,7 +187,6 @@ private:
     void ensure_workspace(uint32_t products);
     void ensure_device_io(uint32_t products);
     void ensure_host_staging(uint32_t products);
-    void multiply_pinned(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
     void bind_ntt();
 
     HostPlan plan_;
@@ -200,12 +201,14 @@ private:
     DeviceBuffer crt_b_, q_, status_;
     DeviceBuffer ws_;
     size_t ws_products_ = 0;
-    // Host-buffer path: double-buffered device inputs/outputs and pinned staging.
-    DeviceBuffer io_dev_[2];
-    PinnedBuffer io_host_[2];
+    // Host-buffer path: kHostSlots device slots for inputs/outputs and pinned staging.
+    static constexpr uint32_t kHostSlots = 3;
+    DeviceBuffer io_dev_[kHostSlots];
+    PinnedBuffer io_host_[kHostSlots];
     size_t io_products_ = 0, io_dev_products_ = 0;
-    cudaEvent_t ev_in_[2] = {}, ev_done_[2] = {}, ev_out_[2] = {};
-    std::vector<cudaEvent_t> piece_ev_[2];   // staged output pieces of each slot
+    cudaEvent_t ev_in_[kHostSlots] = {}, ev_done_[kHostSlots] = {}, ev_out_[kHostSlots] = {};
+    cudaEvent_t ev_host_[kHostSlots] = {};   // staged output landed (waited on by the output worker only)
+    std::unique_ptr<HostWorker> worker_;   // output side of the host path (created on first use)
     NttArgs ntt_{};
     EncodeArgs enc_{};
     CrtArgs crt_{};
@@ -216,6 +219,7 @@ private:
 // the fastest and records it for later Contexts of the same geometry.
 struct AutotuneReport {
     uint32_t group = 0, crt_tiles = 0, crt_persistent = 0, row_rows = 0, row_local = 0, row_bits = 0, candidates = 0;
+    uint32_t row_pass = 0;
     double us_per_product_default = 0, us_per_product_tuned = 0;
 };
 AutotuneReport autotune(Context& ctx, uint32_t max_group);

@@ -57,6 +57,8 @@ struct Tuning {
                               // halved while the grid holds fewer than four CTAs per SM
     uint32_t crt_gap_fold = 1;   // 1: gap-form q (2^W - gap) reduces by folding; 0: generic reduction
     uint32_t row_local = 0;      // row pass elements per thread: 0 default, 3 (8 elements) or 4 (16, R = 256)
+    uint32_t row_pass = 0;       // row pass kernel: 0 row_kernel, 1 row_sliced_kernel (per-row twist tables
+                                 // shared by the products of a CTA's slice); an autotuner candidate
 };
 
 size_t encode_smem_bytes(uint32_t K, uint32_t group_cols);

@@ -1,4 +1,6 @@
 // NTT kernels (see ntt.cuh for the decomposition).
+#include <algorithm>
+
 #include "ntt.cuh"
 #include "kernels.hpp"
 
@@ -275,6 +277,137 @@ row_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t*
     }
 }
 
+// ---------------------------------------------- twisted row pass, sliced --
+// row_kernel's arithmetic with its twist factors taken from per-row tables:
+// tw[s] = tau^s and uw[s] = K tau^-s (K = N^-1 inv(Prod/p) 2^32, consts.w),
+// each with its Shoup companion, built once per CTA for its rows in flight and
+// shared by every product of its slice.  A twist is then one Shoup product
+// instead of two (tau^s = T_lo[e mod Z] T_hi[e / Z]), and the threads of a row
+// read consecutive entries instead of scattered table words.  The cyclic
+// twiddles (and their twiddle-1 butterflies) are row_kernel's.
+
+// floor(w * 2^32 / p) for w < p, 2^30 < p < 2^31, mu = floor(2^62 / p) < 2^32:
+// the estimate floor(w mu / 2^30) is at most 2 below, and the remainder
+// w 2^32 - q p tells how far.
+__device__ __forceinline__ uint32_t shoup_companion(uint32_t w, uint32_t p, uint32_t mu) {
+    uint32_t q = uint32_t((uint64_t(w) * mu) >> 30);
+    uint64_t r = (uint64_t(w) << 32) - uint64_t(q) * p;
+    if (r >= p) { r -= p; ++q; }
+    if (r >= p) ++q;
+    return q;
+}
+
+// One row's twist (tw) and untwist (uw) factors, built by the row's TPR
+// threads (thread t): entry s starts at tau^t (K tau^-t) and steps by
+// tau^TPR (tau^-TPR).
+template <int RB, int RL>
+__device__ __forceinline__ void build_row_twists(uint2* tw, uint2* uw, uint32_t i2, uint32_t t, const NttArgs& a,
+                                                 const uint2* g, uint32_t p, uint32_t mu, uint32_t K, uint32_t Kq) {
+    constexpr uint32_t R = 1u << RB, TPR = R >> RL;
+    const uint32_t two_n = 2 * a.N, zmask = a.Z - 1;
+    auto psi_pow = [&](uint32_t ex) {           // psi^ex for 0 <= ex < 2N
+        const uint2 lo = __ldg(g + a.off_tw_lo + (ex & zmask)), hi = __ldg(g + a.off_tw_hi + (ex >> a.z_bits));
+        return reduce_once(mul_shoup(lo.x, hi.x, hi.y, p), p);
+    };
+    const uint32_t e = 2 * bit_reverse_dev(i2, a.c_bits) + 1;          // tau = psi^e; e * R < 2N
+    const uint32_t et = e * t, es = e * TPR;
+    uint32_t x = psi_pow(et);                                          // tau^t
+    uint32_t y = reduce_once(mul_shoup(psi_pow(et ? two_n - et : 0u), K, Kq, p), p);   // K tau^-t
+    const uint32_t st = psi_pow(es), sti = psi_pow(two_n - es);        // tau^TPR, tau^-TPR
+    const uint32_t stq = shoup_companion(st, p, mu), stiq = shoup_companion(sti, p, mu);
+    for (uint32_t sidx = t; sidx < R; sidx += TPR) {
+        tw[sidx] = make_uint2(x, shoup_companion(x, p, mu));
+        uw[sidx] = make_uint2(y, shoup_companion(y, p, mu));
+        x = reduce_once(mul_shoup(x, st, stq, p), p);
+        y = reduce_once(mul_shoup(y, sti, stiq, p), p);
+    }
+}
+
+// Grid (row blocks, P, product slices): a CTA walks rows_per_cta rows of one
+// prime, RIF rows at a time, and for each such set the products
+// [blockIdx.z * prod_per_cta, ...) of the chain.
+template <int RB, int RL>
+__global__ void __launch_bounds__(32 * kRowWarps)
+row_sliced_kernel(NttArgs a, const uint32_t* planes_a, size_t a_stride, const uint32_t* planes_b, size_t b_stride,
+                  uint32_t* planes_out, size_t out_stride, uint32_t rows_per_cta, uint32_t a_spectral,
+                  uint32_t nprod, uint32_t prod_per_cta) {
+    using S = RowShape<RB, RL>;
+    constexpr uint32_t R = S::R, TPR = S::TPR, RPW = S::RPW, E = 1u << RL;
+    constexpr uint32_t RIF = kRowWarps * RPW;                 // rows in flight per CTA
+    extern __shared__ uint4 smem_raw[];
+    uint2* s_row_f = reinterpret_cast<uint2*>(smem_raw);
+    uint2* s_row_i = s_row_f + R;
+    uint2* s_tabs = s_row_i + R;                               // RIF rows x (twist R, untwist R)
+    uint32_t* xbuf = reinterpret_cast<uint32_t*>(s_tabs + 2 * RIF * R);   // kRowWarps x 2 x kWarpWords words
+
+    const uint32_t j = blockIdx.y;
+    const uint4 pc = a.consts[j];
+    const uint32_t p = pc.x, np = pc.z;
+    const uint32_t mu = uint32_t((uint64_t(1) << 62) / p);
+    const uint32_t K = pc.w, Kq = shoup_companion(K, p, mu);
+    const uint2* g = a.tables + size_t(j) * a.table_stride;
+    for (uint32_t i = threadIdx.x; i < R; i += blockDim.x) {
+        const uint32_t slot = i ? row_tw_slot<RB, RL>(i) : 0u;
+        s_row_f[slot] = g[a.off_row_f + i];
+        s_row_i[slot] = g[a.off_row_i + i];
+    }
+    __syncthreads();
+
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t t = lane % TPR, rw = lane / TPR;
+    const uint32_t rslot = warp * RPW + rw;                    // this thread's row among the rows in flight
+    uint2* tw = s_tabs + size_t(rslot) * 2 * R;                // written and read by this row's warp only
+    uint2* uw = tw + R;
+    uint32_t* bufa = xbuf + warp * 2 * S::kWarpWords + rw * (R + S::kPad);
+    uint32_t* bufb = bufa + S::kWarpWords;
+    const uint32_t C = a.N / R;
+    const size_t jn = size_t(j) * a.N;
+    const uint32_t z0 = blockIdx.z * prod_per_cta;
+    const uint32_t z1 = min(nprod, z0 + prod_per_cta);
+    constexpr PhaseMap<RB, RL> m0(0);
+    constexpr PhaseMap<RB, RL> ml(phase_count(RB, RL) - 1);
+
+    for (uint32_t it = 0; it * RIF < rows_per_cta; ++it) {
+        const uint32_t i2 = blockIdx.x * rows_per_cta + it * RIF + rslot;
+        const bool valid = i2 < C && it * RIF + rslot < rows_per_cta;
+        __syncwarp();                                          // the previous rows' tables are read out
+        if (valid) build_row_twists<RB, RL>(tw, uw, i2, t, a, g, p, mu, K, Kq);
+        __syncwarp();
+        for (uint32_t z = z0; z < z1; ++z) {
+            const uint32_t* rowa = planes_a + z * a_stride + jn + size_t(i2) * R;
+            const uint32_t* rowb = planes_b + z * b_stride + jn + size_t(i2) * R;
+            uint32_t* rowo = planes_out + z * out_stride + jn + size_t(i2) * R;
+            uint32_t x[E], xb[E];
+#pragma unroll
+            for (uint32_t k = 0; k < E; ++k) {
+                // A cached in spectral form is stored in natural order (element s at s).
+                x[k] = valid ? rowa[a_spectral ? ml.index(t, k) : m0.index(t, k)] : 0u;
+                xb[k] = valid ? rowb[m0.index(t, k)] : 0u;
+            }
+#pragma unroll
+            for (uint32_t k = 0; k < E; ++k) {
+                const uint2 w = tw[m0.index(t, k)];
+                if (!a_spectral) x[k] = mul_shoup(x[k], w.x, w.y, p);
+                xb[k] = mul_shoup(xb[k], w.x, w.y, p);
+            }
+            if (!a_spectral) row_forward<RB, RL>(x, bufa, t, p, s_row_f);
+            row_forward<RB, RL>(xb, bufb, t, p, s_row_f);
+#pragma unroll
+            for (uint32_t k = 0; k < E; ++k) x[k] = mul_mont(reduce_once(x[k], p), xb[k], p, np);
+            row_inverse<RB, RL>(x, bufa, t, p, s_row_i);
+#pragma unroll
+            for (uint32_t k = 0; k < E; ++k) {
+                const uint32_t sidx = m0.index(t, k);
+                const uint2 w = uw[sidx];
+                uint32_t v = mul_shoup(x[k], w.x, w.y, p);
+                // With a single row there is no inverse column pass: emit canonical terms here.
+                if (C == 1) v = reduce_once(v, p);
+                if (valid) rowo[sidx] = v;
+            }
+        }
+    }
+}
+
 // Forward row transform only (twist + cyclic NTT), in place: leaves an operand
 // in the spectral form that row_kernel accepts with a_spectral = 1.
 template <int RB, int RL>
@@ -396,9 +529,53 @@ size_t row_smem_bytes(const NttArgs& a, bool forward_only) {
     return tabs * sizeof(uint2) + (forward_only ? 1 : 2) * kRowWarps * warp_words * sizeof(uint32_t);
 }
 
+size_t row_sliced_smem_bytes(const NttArgs& a) {
+    const uint32_t R = a.R;
+    const uint32_t rl = row_local_bits(a);
+    const uint32_t rpw = 32 / (R >> rl);
+    const size_t warp_words = size_t(rpw) * (R + (rl == 4 ? 16 : 0));
+    const size_t rif = size_t(kRowWarps) * rpw;
+    return (2 * R + 2 * rif * R) * sizeof(uint2) + 2 * kRowWarps * warp_words * sizeof(uint32_t);
+}
+
+// The sliced row pass: a CTA per (row set, prime, product slice); slices of
+// at least two products, so that each row's tables serve several products,
+// and enough CTAs for four per SM where the chain allows.
+static cudaError_t launch_row_sliced(const NttArgs& a, const uint32_t* planes_a, size_t a_stride,
+                                     const uint32_t* planes_b, size_t b_stride, uint32_t* planes_out,
+                                     size_t out_stride, uint32_t nprod, bool a_spectral, cudaStream_t st) {
+    const uint32_t R = a.R;
+    const uint32_t C = a.N / R;
+    const uint32_t rif = kRowWarps * (32 / (R >> row_local_bits(a)));
+    uint32_t rows = a.row_rows ? (a.row_rows + rif - 1) / rif * rif : rif;
+    if (rows > (C + rif - 1) / rif * rif) rows = (C + rif - 1) / rif * rif;
+    const uint32_t xy = (C + rows - 1) / rows * a.P;
+    const uint32_t want = 4 * sm_count();
+    uint32_t slices = std::max<uint32_t>(1, std::min<uint32_t>(nprod / 2, (want + xy - 1) / xy));
+    const uint32_t per = (nprod + slices - 1) / slices;
+    slices = (nprod + per - 1) / per;
+    const dim3 grid((C + rows - 1) / rows, a.P, slices);
+    const size_t smem = row_sliced_smem_bytes(a);
+    const uint32_t rb = 31 - __builtin_clz(R) + (row_local_bits(a) == 4 ? 8 : 0);
+    switch (rb) {
+#define BCG_ROWS(RBV, RLV) case RBV + (RLV == 4 ? 8 : 0): { \
+        cudaError_t e = cudaFuncSetAttribute(row_sliced_kernel<RBV, RLV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
+        if (e != cudaSuccess) return e; \
+        row_sliced_kernel<RBV, RLV><<<grid, 32 * kRowWarps, smem, st>>>(a, planes_a, a_stride, planes_b, b_stride, \
+            planes_out, out_stride, rows, a_spectral ? 1u : 0u, nprod, per); break; }
+        BCG_ROWS(4, 3) BCG_ROWS(5, 3) BCG_ROWS(6, 3) BCG_ROWS(7, 3) BCG_ROWS(8, 3) BCG_ROWS(8, 4)
+#undef BCG_ROWS
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_t a_stride,
                                const uint32_t* planes_b, size_t b_stride, uint32_t* planes_out,
                                size_t out_stride, uint32_t nprod, bool a_spectral, cudaStream_t st) {
+    if (a.row_pass == 1)
+        return launch_row_sliced(a, planes_a, a_stride, planes_b, b_stride, planes_out, out_stride, nprod,
+                                 a_spectral, st);
     const uint32_t R = a.R;
     const uint32_t C = a.N / R;
     const uint32_t rpi = kRowWarps * (32 / (R >> row_local_bits(a)));

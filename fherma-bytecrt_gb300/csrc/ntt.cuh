@@ -26,7 +26,7 @@
 namespace bcg {
 
 struct NttArgs {
-    const uint4* consts;       // per prime: p, p^-1, -p^-1, 0
+    const uint4* consts;       // per prime: p, p^-1, -p^-1, N^-1 * inv(Prod/p) * 2^32 mod p
     const uint2* tables;       // per prime: table_stride entries (value, Shoup companion)
     uint32_t table_stride;
     uint32_t off_col_f, off_col_i, off_row_f, off_row_i;
@@ -35,6 +35,7 @@ struct NttArgs {
     uint32_t R;                // row length of the split N = C * R
     uint32_t row_rows;         // rows of the row pass per CTA (0: the launcher's default)
     uint32_t row_local;        // log2 elements per thread in the row pass (0: 4 for R = 256, else 3)
+    uint32_t row_pass;         // 0: row_kernel; 1: row_sliced_kernel (per-row twist tables)
 };
 
 // Bit positions handled inside one thread during phase `phase` of a transform

@@ -331,6 +331,8 @@ HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw, uint3
         // pointwise product divides by 2^32).
         const uint32_t r32 = uint32_t((uint64_t(1) << 32) % pj);
         const uint32_t K = uint32_t(uint64_t(plan.n_inverse[j]) * plan.crt_inverse[j] % pj * r32 % pj);
+        // The sliced row pass builds its untwist factors K tau^-s from this constant.
+        plan.prime_consts[4 * j + 3] = K;
         for (uint32_t lo = 0; lo < g.Z; ++lo) {
             put(off.tw_lo + lo, lo);
             put(off.itw_lo + lo, two_n - lo);

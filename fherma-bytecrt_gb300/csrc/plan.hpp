@@ -35,7 +35,8 @@ struct HostPlan {
     std::vector<uint32_t> q;               // L words
     std::vector<uint32_t> primes, psi, crt_inverse, n_inverse;
     std::vector<uint32_t> weights;         // (P+1) x L words: (Prod/p_j) mod q, then (-Prod) mod q
-    std::vector<uint32_t> prime_consts;    // 4 words per prime: p, p^-1 mod 2^32, -p^-1 mod 2^32, 0
+    std::vector<uint32_t> prime_consts;    // 4 words per prime: p, p^-1 mod 2^32, -p^-1 mod 2^32,
+                                           // N^-1 * inv(Prod/p) * 2^32 mod p
     std::vector<uint32_t> ntt_tables;      // P x table_stride x (value, Shoup companion)
     std::vector<uint16_t> enc_b;           // fp16 bit patterns, chunked core-matrix order
     std::vector<uint16_t> crt_b;           // fp16 bit patterns, chunked core-matrix order

@@ -47,7 +47,7 @@ class bcg_profile(ctypes.Structure):
 class bcg_autotune_report(ctypes.Structure):
     _fields_ = [("group", ctypes.c_uint32), ("crt_tiles", ctypes.c_uint32), ("row_rows", ctypes.c_uint32),
                 ("row_bits", ctypes.c_uint32), ("candidates", ctypes.c_uint32), ("crt_persistent", ctypes.c_uint32),
-                ("row_local", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("row_local", ctypes.c_uint32), ("row_pass", ctypes.c_uint32),
                 ("us_per_product_default", ctypes.c_double), ("us_per_product_tuned", ctypes.c_double)]
 
 

@@ -93,6 +93,11 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *   "row_local"  row pass elements per thread: 0 (default: 16 for R = 256, else 8),
  *                3 (8) or 4 (16, R = 256 only)
  *   "row_rows"   rows per row-pass CTA; 0: up to 128 with 16 elements per thread, else 32
+ *                (row_pass 1: one set of rows in flight, 16 with 16 elements per thread)
+ *   "row_pass"   0 (default): the row pass twists each element by tau^s with two
+ *                table products; 1: the sliced row pass, whose CTAs build each
+ *                row's twist and untwist factors once and share them with every
+ *                product of their slice (one product per twist)
  *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
  *                Re-plans the twiddle and twist tables (the primes stay).
  *   "wait_limit_ns"  limit of a kernel's wait on another warp role's arrival,
@@ -110,7 +115,7 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
 int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value);
 int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* value);
 /* Autotuner: times whole launch chains on synthetic operands for every value
- * of row_bits, then the CRT kernel and tile shape, row_local, row_rows and group (coordinate search, at most
+ * of row_bits, then the CRT kernel and tile shape, row_local, row_pass, row_rows and group (coordinate search, at most
  * max_group products per chain and 4 GB of workspace), keeps the fastest, and
  * records it so that contexts of the same geometry created later in the
  * process (including those of bcg_batch and bcg_server) start from it.  The
@@ -119,23 +124,27 @@ typedef struct bcg_autotune_report {
     uint32_t group, crt_tiles, row_rows, row_bits;
     uint32_t candidates;    /* settings timed */
     uint32_t crt_persistent;
-    uint32_t row_local, reserved;
+    uint32_t row_local, row_pass;
     double us_per_product_default, us_per_product_tuned;
 } bcg_autotune_report;
 int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_report* out);
 
 /* ---- whole products.
  * bcg_multiply: host buffers, synchronous; replaces fherma_run
- * (native-smoke/solve.cu:506-525; batched native-batched/solve.cu:200-244). */
+ * (native-smoke/solve.cu:506-525; batched native-batched/solve.cu:200-244).
+ * Pageable buffers are page-locked for the duration of the call (and
+ * unlocked before it returns), so that every copy is asynchronous. */
 int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
 /* Like bcg_multiply, but the product ([count][N][L] words) is handed over in
  * order, in consecutive runs, to sink(user, words, n) as each run arrives on
  * the host; `words` is valid only during the call, and the sink must not
- * throw.  Once, while the first products compute, the sink is called with
- * words == NULL and n = the words that will arrive first: a chance to prepare
- * the destination (the plugin faults in its output pages then).  For callers
- * that build their own output container (the plugin's owned std::vector)
- * without filling it first.  No counterpart in the reference. */
+ * throw.  The products travel in groups; before the runs of each group the
+ * sink is called with words == NULL and n = the group's words: a chance to
+ * prepare the destination (the plugin faults in its output pages then).  The
+ * sink is called from a library thread, one call at a time, while the calling
+ * thread already issues the next groups.  For callers that build their own
+ * output container (the plugin's owned std::vector) without filling it first.
+ * No counterpart in the reference. */
 typedef void (*bcg_sink)(void* user, const uint32_t* words, size_t n);
 int bcg_multiply_sink(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t count, bcg_sink sink,
                       void* user);

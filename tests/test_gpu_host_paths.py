@@ -74,13 +74,23 @@ def test_sink_pieces_arrive_in_order(N, W, count):
     def sink(words, n):
         calls.append((words is None, n))
         if words is not None:
-            assert words.shape == (n,) and n <= (4 << 20) // 4
+            assert words.shape == (n,)
             pieces.append(words.copy())
 
     m.multiply_sink(a, b, sink)
-    # One preparation call first, with the words of the first group.
-    assert calls[0][0] and 0 < calls[0][1] <= a.size
-    assert sum(1 for prep, _ in calls if prep) == 1
+    # Each group's words are announced by a preparation call (words=None, n =
+    # the group's words), then arrive in pieces that add up to exactly n.
+    assert calls[0][0]
+    left = 0
+    for prep, n in calls:
+        if prep:
+            assert left == 0 and n > 0
+            left = n
+        else:
+            left -= n
+            assert left >= 0
+    assert left == 0
+    assert sum(n for prep, n in calls if prep) == a.size
     got = np.concatenate(pieces).reshape(a.shape)
     assert np.array_equal(got, device_products(m, a, b))
     m.close()

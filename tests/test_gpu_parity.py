@@ -179,29 +179,38 @@ def test_plugin_abi_roundtrip():
 
 @pytest.mark.parametrize("N,W", [(16, 40), (64, 100), (2048, 300), (16384, 434), (32768, 868), (65536, 1747)])
 def test_tuning_knobs_stay_bit_exact(N, W):
-    """Every CRT kernel and tile shape and every row-pass CTA shape gives the oracle's product."""
+    """Every CRT kernel and tile shape and every row-pass kernel and CTA shape gives the oracle's product."""
     pkg = package()
     m, o, q = setup(N, W, 1)
     a = np.stack([pkg.inputs.uniform(q, N, 70 + i) for i in range(3)])
     b = np.stack([pkg.inputs.uniform(q, N, 80 + i) for i in range(3)])
     want = [o.multiply(a[i], b[i]) for i in range(3)]
     da, db = dev(a), dev(b)
-    for persistent, tiles, rows, local in ((0, 1, 0, 3), (0, 2, 8, 0), (0, 1, 64, 3), (1, 2, 0, 0), (1, 2, 64, 0),
-                                           (1, 2, 128, 3)):
+    for persistent, tiles, rows, local, rpass in ((0, 1, 0, 3, 0), (0, 2, 8, 0, 1), (0, 1, 64, 3, 1),
+                                                  (1, 2, 0, 0, 0), (1, 2, 64, 0, 1), (1, 2, 128, 3, 0),
+                                                  (1, 2, 0, 3, 1), (1, 2, 16, 0, 1), (1, 2, 0, 0, 1)):
         m.set_tuning("crt_persistent", persistent)
         m.set_tuning("crt_tiles", tiles)
         m.set_tuning("row_rows", rows)
         m.set_tuning("row_local", local)
+        m.set_tuning("row_pass", rpass)
         for rep in range(2):
             out = torch.zeros_like(da)
             m.multiply_device(da, db, out, 3)
             m.synchronize()
             for i in range(3):
-                assert np.array_equal(host(out[i]), want[i]), (persistent, tiles, rows, rep, i)
+                assert np.array_equal(host(out[i]), want[i]), (persistent, tiles, rows, local, rpass, rep, i)
+    # One product per chain through the sliced row pass.
+    m.set_tuning("row_pass", 1)
+    out = torch.zeros_like(da[:1])
+    m.multiply_device(da[:1], db[:1], out, 1)
+    m.synchronize()
+    assert np.array_equal(host(out[0]), want[0])
     m.set_tuning("crt_persistent", 1)
     m.set_tuning("crt_tiles", 2)
     m.set_tuning("row_rows", 0)
     m.set_tuning("row_local", 0)
+    m.set_tuning("row_pass", 0)
 
 
 @pytest.mark.parametrize("N,W", [(1024, 200), (4096, 868), (32768, 868)])
@@ -220,10 +229,12 @@ def test_radix_splits_stay_bit_exact(N, W):
             continue
         m.set_tuning("row_bits", rb)
         assert m.get_tuning("row_bits") == rb
-        out = torch.zeros((1, N, len(q)), dtype=torch.int32, device="cuda")
-        m.multiply_device(dev(a[None]), dev(b[None]), out, 1)
-        m.synchronize()
-        assert np.array_equal(host(out[0]), want), rb
+        for rpass in (0, 1):                     # both row passes
+            m.set_tuning("row_pass", rpass)
+            out = torch.zeros((1, N, len(q)), dtype=torch.int32, device="cuda")
+            m.multiply_device(dev(a[None]), dev(b[None]), out, 1)
+            m.synchronize()
+            assert np.array_equal(host(out[0]), want), (rb, rpass)
         tried += 1
     assert tried >= 2
     m.close()
@@ -238,14 +249,14 @@ def test_autotune_applies_and_is_remembered():
     assert r["candidates"] >= 5
     assert 0 < r["us_per_product_tuned"] <= r["us_per_product_default"] * 1.05
     assert r["crt_tiles"] in (1, 2) and 1 <= r["group"] <= 8
-    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits"):
+    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits", "row_pass"):
         assert m.get_tuning(knob) == r[knob], knob
     a, b = pkg.inputs.uniform(q, N, 3), pkg.inputs.uniform(q, N, 4)
     assert np.array_equal(m.multiply(a, b), O.Oracle(N, W, q).multiply(a, b))
     # Another context of the same geometry (another q) starts from the tuned shapes.
     q2 = pkg.inputs.modulus(W, 32)
     m2 = pkg.Multiplier(N, W, q2)
-    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits"):
+    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits", "row_pass"):
         assert m2.get_tuning(knob) == r[knob], knob
     a2, b2 = pkg.inputs.uniform(q2, N, 5), pkg.inputs.uniform(q2, N, 6)
     assert np.array_equal(m2.multiply(a2, b2), O.Oracle(N, W, q2).multiply(a2, b2))
