@@ -10,9 +10,12 @@
 #include "fherma.h"
 #include "bytecrt_gb300.h"
 
+#include <cstdlib>
 #include <cstring>
 #include <exception>
+#include <malloc.h>
 #include <memory>
+#include <mutex>
 #include <omp.h>
 #include <sys/mman.h>
 #include <unistd.h>
@@ -64,6 +67,23 @@ void populate(void* p, size_t n) {
     }
 }
 
+// The owned output of every call is a fresh vector of up to 1.8 GB.  glibc
+// serves such blocks with mmap and unmaps them when they are freed, so every
+// call would fault in fresh pages; while copies and kernels run, those faults
+// cost 33 ms per B = 128 call on a GB300 host (9 ms on an idle one).  Serving
+// large blocks from the heap and keeping freed heap memory mapped lets the next
+// output land on pages that are already there.  Process-wide; switched off by
+// BYTECRT_KEEP_HEAP=0 for processes that must hand memory back to the system.
+void keep_heap_mapped() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char* env = std::getenv("BYTECRT_KEEP_HEAP");
+        if (env && env[0] == '0') return;
+        mallopt(M_MMAP_MAX, 0);          // large blocks from the heap, not mmap
+        mallopt(M_TRIM_THRESHOLD, -1);   // freed heap memory stays mapped
+    });
+}
+
 bool disjoint(const void* dst, const void* src, size_t n) {
     const char* d = static_cast<const char*>(dst);
     const char* s = static_cast<const char*>(src);
@@ -103,6 +123,7 @@ void check(int rc, const char* what) {
 }  // namespace
 
 void* fherma_init(const fherma::Point& p) {
+    keep_heap_mapped();
     auto s = std::make_unique<State>();
 #ifdef FHERMA_BATCHED
     if (p.B == 0 || p.B > 128) throw std::runtime_error("bytecrt-gb300 batch coverage B=1..128");
