@@ -274,12 +274,21 @@ def host_cpu() -> dict:
                     break
     except OSError:
         pass
-    if model is None:
-        try:   # Arm: the SoC name, else the implementer/part codes
-            with open("/sys/devices/soc0/machine") as f:
-                model = f.read().strip()
+    if model is None:   # Arm: the implementer and part codes (0x41/0xd4f: Arm Neoverse V2, as in Grace)
+        codes = {}
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if ":" in line:
+                        k, v = (x.strip() for x in line.split(":", 1))
+                        if k in ("CPU implementer", "CPU part") and k not in codes:
+                            codes[k] = v
         except OSError:
-            model = platform.processor() or platform.machine()
+            pass
+        names = {("0x41", "0xd4f"): "Arm Neoverse V2", ("0x41", "0xd40"): "Arm Neoverse V1",
+                 ("0x41", "0xd0c"): "Arm Neoverse N1"}
+        key = (codes.get("CPU implementer"), codes.get("CPU part"))
+        model = names.get(key) or (f"implementer {key[0]} part {key[1]}" if key[0] else platform.machine())
     mask = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else list(range(os.cpu_count() or 1))
     cores = set()
     for cpu in mask:

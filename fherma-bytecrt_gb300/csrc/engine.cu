@@ -126,6 +126,7 @@ Context::~Context() {
         if (ev_done_[s]) cudaEventDestroy(ev_done_[s]);
         if (ev_out_[s]) cudaEventDestroy(ev_out_[s]);
         if (ev_host_[s]) cudaEventDestroy(ev_host_[s]);
+        for (cudaEvent_t e : piece_ev_[s]) cudaEventDestroy(e);
     }
     if (copy_in_) cudaStreamDestroy(copy_in_);
     if (copy_out_) cudaStreamDestroy(copy_out_);
@@ -200,22 +201,23 @@ void Context::ensure_workspace(uint32_t products) {
     ws_products_ = products;
 }
 
-void Context::ensure_device_io(uint32_t products) {
-    if (products <= io_dev_products_) return;
-    cudaStreamSynchronize(stream_);
-    cudaStreamSynchronize(copy_in_);
-    cudaStreamSynchronize(copy_out_);
-    const size_t bytes = size_t(products) * coeff_words() * 4 * 3;
-    for (uint32_t s = 0; s < kHostSlots; ++s) io_dev_[s].allocate(bytes);
-    io_dev_products_ = products;
-}
-
-void Context::ensure_host_staging(uint32_t products) {
-    ensure_device_io(products);
-    if (products <= io_products_) return;
-    const size_t bytes = size_t(products) * coeff_words() * 4 * 3;
-    for (uint32_t s = 0; s < kHostSlots; ++s) io_host_[s].allocate(bytes);
-    io_products_ = products;
+// Host-path slots, allocated only as far as a call uses them (a call of n
+// groups uses min(n, kHostSlots) slots): device [A | B | C]; pinned A | B
+// where operands are packed for the device (the GPU cannot read them in
+// place); pinned C where products go to a sink or an unlocked output.
+void Context::ensure_host_slots(uint32_t products, uint32_t slots, bool pack_in, bool stage_out) {
+    const size_t unit = size_t(products) * coeff_words() * 4;
+    auto grow = [&](auto& buf, size_t bytes, cudaStream_t st) {
+        if (buf.bytes >= bytes) return;
+        cudaStreamSynchronize(stream_);
+        cudaStreamSynchronize(st);
+        buf.allocate(bytes);
+    };
+    for (uint32_t s = 0; s < slots; ++s) {
+        grow(io_dev_[s], 3 * unit, copy_out_);
+        if (pack_in) grow(io_in_[s], 2 * unit, copy_in_);
+        if (stage_out) grow(io_out_[s], unit, copy_out_);
+    }
 }
 
 void Context::encode(const uint32_t* a, const uint32_t* b, uint32_t* pa, uint32_t* pb, size_t plane_stride,
@@ -571,11 +573,18 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     } quiesce{copy_in_, stream_, copy_out_};
     const bool out_pinned = !sink && is_pinned(c);
     ensure_workspace(g);
-    if (out_pinned && (pageable_direct_ || (is_pinned(a) && is_pinned(b)))) ensure_device_io(g);
-    else ensure_host_staging(g);
     const uint32_t ngroups = (count + g - 1) / g;
-    auto group_size = [&](uint32_t gi) { return std::min(g, count - gi * g); };
+    const uint32_t slots = std::min(kHostSlots, ngroups);
     constexpr size_t kPiece = size_t(4) << 20;
+    ensure_host_slots(g, slots, !pageable_direct_ && !(is_pinned(a) && is_pinned(b)), !out_pinned);
+    const size_t max_pieces = (size_t(g) * cw * 4 + kPiece - 1) / kPiece;
+    for (uint32_t s = 0; s < slots; ++s)
+        while (piece_ev_[s].size() < max_pieces) {
+            cudaEvent_t e;
+            check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            piece_ev_[s].push_back(e);
+        }
+    auto group_size = [&](uint32_t gi) { return std::min(g, count - gi * g); };
     auto stage_in = [&](ChunkLock& lk, uint32_t gi, char* h, char* d, const char* x, size_t bytes) {
         if (lk.usable(gi)) {                   // pinned or locked: asynchronous
             lk.copy_to_device(d, gi, bytes, copy_in_);
@@ -598,7 +607,12 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     uint32_t issued = 0, drained = 0;
     bool stop = false;
     std::exception_ptr out_error;
-    if (!out_pinned) {
+    // One or two groups leave nothing to overlap on the host: their products
+    // come back in 4 MiB pieces that this thread hands over as each lands (one
+    // product through the plugin: 0.71 ms through the worker, 0.5 ms so).
+    const bool inline_out = !out_pinned && ngroups <= 2;
+    const bool worker_out = !out_pinned && !inline_out;
+    if (worker_out) {
         if (!worker_) worker_ = std::make_unique<HostWorker>();
         worker_->post([&] {
             try {
@@ -608,9 +622,9 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
                         cv.wait(lk, [&] { return issued > gi || stop; });
                         if (issued <= gi) return;
                     }
-                    const uint32_t s = gi % kHostSlots;
+                    const uint32_t s = gi % slots;
                     const size_t bytes = size_t(group_size(gi)) * cw * 4;
-                    const uint32_t* src = io_host_[s].as<uint32_t>() + 2 * g * cw;
+                    const uint32_t* src = io_out_[s].as<uint32_t>();
                     // The products of this group are on their way: the sink may prepare room for them.
                     if (sink) sink(user, nullptr, bytes / 4);
                     check(cudaEventSynchronize(ev_host_[s]), "output copy");
@@ -637,32 +651,32 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
             cv.notify_all();
             w->wait();
         }
-    } settle{out_pinned ? nullptr : worker_.get(), mu, cv, stop};
+    } settle{worker_out ? worker_.get() : nullptr, mu, cv, stop};
 
     for (uint32_t gi = 0; gi < ngroups; ++gi) {
-        const uint32_t s = gi % kHostSlots;
+        const uint32_t s = gi % slots;
         const uint32_t n = group_size(gi);
         const size_t off = size_t(gi) * g * cw, bytes = size_t(n) * cw * 4;
-        if (!out_pinned && gi >= kHostSlots) {
+        if (worker_out && gi >= slots) {
             // The slot's previous group has left its staging (and so its device output).
             std::unique_lock<std::mutex> lk(mu);
-            cv.wait(lk, [&] { return drained + kHostSlots > gi || out_error; });
+            cv.wait(lk, [&] { return drained + slots > gi || out_error; });
             if (out_error) break;
         }
         lock_a.lock_through(gi);
         lock_b_or_a.lock_through(gi);
         uint32_t* d = io_dev_[s].as<uint32_t>();
-        uint32_t* h = io_host_[s].ptr ? io_host_[s].as<uint32_t>() : nullptr;
+        uint32_t* h = io_in_[s].ptr ? io_in_[s].as<uint32_t>() : nullptr;
         // Packing into the slot's staging: its previous inputs have left for the device.
         const bool packs = !pageable_direct_ && !(lock_a.usable(gi) && lock_b_or_a.usable(gi));
-        if (packs && gi >= kHostSlots) check(cudaEventSynchronize(ev_in_[s]), "slot reuse");
-        if (gi >= kHostSlots) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
+        if (packs && gi >= slots) check(cudaEventSynchronize(ev_in_[s]), "slot reuse");
+        if (gi >= slots) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
         // Operand A first: the device encodes it while operand B comes in.
         stage_in(lock_a, gi, reinterpret_cast<char*>(h), reinterpret_cast<char*>(d),
                  reinterpret_cast<const char*>(a + off), bytes);
         check(cudaEventRecord(ev_in_[s], copy_in_), "event");
         check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
-        if (gi >= kHostSlots) check(cudaStreamWaitEvent(stream_, ev_out_[s], 0), "slot reuse");
+        if (gi >= slots) check(cudaStreamWaitEvent(stream_, ev_out_[s], 0), "slot reuse");
         chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_, nullptr, [&] {
             stage_in(lock_b_or_a, gi, reinterpret_cast<char*>(h ? h + g * cw : nullptr),
                      reinterpret_cast<char*>(d + g * cw), reinterpret_cast<const char*>(b + off), bytes);
@@ -671,19 +685,43 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         });
         check(cudaEventRecord(ev_done_[s], stream_), "event");
         check(cudaStreamWaitEvent(copy_out_, ev_done_[s], 0), "event wait");
-        check(cudaMemcpyAsync(out_pinned ? c + off : h + 2 * g * cw, d + 2 * g * cw, bytes, cudaMemcpyDeviceToHost,
-                              copy_out_), "output copy");
+        if (inline_out) {
+            char* hs = reinterpret_cast<char*>(io_out_[s].as<uint32_t>());
+            const char* ds = reinterpret_cast<const char*>(d + 2 * g * cw);
+            for (size_t k = 0, po = 0; po < bytes; ++k, po += kPiece) {
+                check(cudaMemcpyAsync(hs + po, ds + po, std::min(kPiece, bytes - po), cudaMemcpyDeviceToHost,
+                                      copy_out_), "output copy");
+                check(cudaEventRecord(piece_ev_[s][k], copy_out_), "event");
+            }
+        } else {
+            check(cudaMemcpyAsync(out_pinned ? c + off : io_out_[s].as<uint32_t>(), d + 2 * g * cw, bytes,
+                                  cudaMemcpyDeviceToHost, copy_out_), "output copy");
+        }
         check(cudaEventRecord(ev_out_[s], copy_out_), "event");
         // Lock the next group's inputs while the device works on this one.
         lock_a.lock_through(gi + 1);
         lock_b_or_a.lock_through(gi + 1);
-        if (out_pinned) continue;
+        if (!worker_out) continue;
         check(cudaEventRecord(ev_host_[s], copy_out_), "event");
         std::lock_guard<std::mutex> lk(mu);
         issued = gi + 1;
         cv.notify_all();
     }
-    if (!out_pinned) {
+    if (inline_out) {
+        for (uint32_t gi = 0; gi < ngroups; ++gi) {
+            const uint32_t s = gi % slots;
+            const size_t bytes = size_t(group_size(gi)) * cw * 4;
+            const char* src = reinterpret_cast<const char*>(io_out_[s].as<uint32_t>());
+            char* dst = reinterpret_cast<char*>(c + size_t(gi) * g * cw);
+            if (sink) sink(user, nullptr, bytes / 4);
+            for (size_t k = 0, po = 0; po < bytes; ++k, po += kPiece) {
+                const size_t pn = std::min(kPiece, bytes - po);
+                check(cudaEventSynchronize(piece_ev_[s][k]), "output copy");
+                if (sink) sink(user, reinterpret_cast<const uint32_t*>(src + po), pn / 4);
+                else parallel_copy(dst + po, src + po, pn);
+            }
+        }
+    } else if (worker_out) {
         {
             std::unique_lock<std::mutex> lk(mu);
             cv.wait(lk, [&] { return drained == ngroups || out_error; });
