@@ -501,6 +501,7 @@ def run_native(args):
     del a_h, b_h, c_h
 
     uneven = run_uneven(pkg, args, stream, local) if args.uneven else None
+    encode_kernels = run_encode_kernels(pkg, stream, local) if args.encode_kernels and rank == 0 else None
     served = run_served(pkg, args, local, value, e2e_value) if args.served else None
 
     if rank != 0:
@@ -574,6 +575,7 @@ def run_native(args):
                   "batched_over_plain_device": value / world / (1000.0 / plain_ms),
                   "batched_over_plain_e2e": e2e_value / world / (1000.0 / plain_e2e_ms)},
         "uneven": uneven,
+        "encode_kernels": encode_kernels,
         "served": served,
         "plugin": plugin,
         "roofline": roofline,
@@ -586,6 +588,55 @@ def run_native(args):
     batch.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_encode_kernels(pkg, stream, device=0):
+    """The two encode kernels at the points where the CUDA-core one applies
+    (L <= 32): microseconds per product for the encode alone, with one product
+    per launch and with the point's default chain length, and for the whole
+    chain through each.  Both encoders' whole products are checked equal."""
+    import numpy as np
+    import torch
+    out = {}
+    for n, w in ((1024, 64), (4096, 200), (16384, 434), (32768, 868)):
+        q = pkg.inputs.modulus(w, 5)
+        m = pkg.Multiplier(n, w, q, device=device)
+        group = m.get_tuning("group")
+        cw, pw = n * m.L, m.plane_words
+        a = torch.from_numpy(np.stack([pkg.inputs.uniform(q, n, 10 + i) for i in range(group)]).view(np.int32)).cuda()
+        b = torch.from_numpy(np.stack([pkg.inputs.uniform(q, n, 50 + i) for i in range(group)]).view(np.int32)).cuda()
+        pa = torch.empty(group * pw, dtype=torch.int32, device="cuda")
+        pb = torch.empty_like(pa)
+        c = torch.empty((group, n, m.L), dtype=torch.int32, device="cuda")
+        row = {"N": n, "W": w, "L": m.L, "P": m.P, "group": group}
+        products = {}
+        for kind in ("tcgen05", "scalar"):
+            m.set_tuning("encode_scalar", 1 if kind == "scalar" else 0)
+
+            def per_product(fn, count, iters):
+                for _ in range(3):
+                    fn()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+                for _ in range(iters):
+                    fn()
+                e.record(stream)
+                torch.cuda.synchronize()
+                return 1000.0 * s.elapsed_time(e) / (iters * count)
+
+            cs = stream.cuda_stream
+            row[kind] = {
+                "encode_us_1": per_product(lambda: m.encode_device(a, b, pa, pb, pw, 1, stream=cs), 1, 50),
+                "encode_us_chain": per_product(lambda: m.encode_device(a, b, pa, pb, pw, group, stream=cs),
+                                               group, 20),
+                "chain_us": per_product(lambda: m.multiply_device(a, b, c, group, stream=cs), group, 10),
+            }
+            m.synchronize()
+            products[kind] = c.cpu()
+        row["same_products"] = bool(torch.equal(products["tcgen05"], products["scalar"]))
+        out[f"{n}/{w}"] = row
+        m.close()
+    return out
 
 
 def run_plugin(pkg, args, device=0):
@@ -955,9 +1006,11 @@ def main():
                     help="parallel branches of the timed batch graph that launch chains alternate over (the "
                          "profiled pass for the rooflines always runs one branch)")
     ap.add_argument("--no-served", dest="served", action="store_false", help="skip the served sweep")
+    ap.add_argument("--no-encode-kernels", dest="encode_kernels", action="store_false",
+                    help="skip comparing the tcgen05 and CUDA-core encoders at small-L points")
     ap.add_argument("--no-plugin", dest="plugin", action="store_false",
                     help="skip timing the plugin harness binaries")
-    ap.add_argument("--plugin-cases", type=int, default=3, help="cases of the B=128 plugin run")
+    ap.add_argument("--plugin-cases", type=int, default=5, help="cases of the B=128 plugin run")
     ap.add_argument("--served-loads", default="0.25,0.5,0.75,0.9",
                     help="offered loads as fractions of the estimated capacity")
     ap.add_argument("--served-seconds", type=float, default=1.5, help="arrival window per offered load")

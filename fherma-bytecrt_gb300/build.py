@@ -23,7 +23,7 @@ SHIM = os.path.join(HERE, "libfherma_gb300.so")
 HARNESS = os.path.join(HERE, "solution")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CORE_SOURCES = ["plan.cu", "encode.cu", "ntt.cu", "crt.cu", "crt_persistent.cu", "engine.cu", "capi.cu", "static_scratch.cu", "autotune.cu",
+CORE_SOURCES = ["plan.cu", "encode.cu", "encode_scalar.cu", "ntt.cu", "crt.cu", "crt_persistent.cu", "engine.cu", "capi.cu", "static_scratch.cu", "autotune.cu",
                 "batch.cu", "server.cu", "capi_serve.cu"]
 
 
@@ -77,7 +77,7 @@ def build(verbose: bool = False) -> str:
         if _stale(shim, [shim_src, LIB, *_headers()]):
             tmp = shim + f".tmp{os.getpid()}"
             subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-Wl,--wrap=memcpy",
-                            "-Wl,--wrap=memmove", *defs, *inc, "-o", tmp, shim_src,
+                            "-Wl,--wrap=memmove", "-Wl,--wrap=memset", *defs, *inc, "-o", tmp, shim_src,
                             "-L", HERE, "-lbytecrt_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
             os.replace(tmp, shim)
         harness = os.path.join(HERE, f"solution{suffix}")

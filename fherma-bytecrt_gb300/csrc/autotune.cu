@@ -1,6 +1,6 @@
-// Per-geometry autotuner: picks the NTT radix split, the CRT MMA tile shape,
-// the row-pass CTA shape and the products per launch chain by timing whole
-// launch chains on the device.
+// Per-geometry autotuner: picks the encode kernel, the NTT radix split, the CRT
+// MMA tile shape, the row-pass CTA shape and the products per launch chain by
+// timing whole launch chains on the device.
 //
 // The reference fixes its shapes per geometry by hand (native-smoke/solve.cu
 // instantiates one kernel set per (N, P, Kpad)); here the search runs once per
@@ -26,10 +26,11 @@ std::map<Key, AutotuneReport>& tuned() {
 }
 
 struct Settings {
-    uint32_t row_bits, crt_tiles, crt_persistent, row_rows, row_local, group, row_pass;
+    uint32_t row_bits, crt_tiles, crt_persistent, row_rows, row_local, group, row_pass, encode_scalar;
     bool operator==(const Settings& o) const {
         return row_bits == o.row_bits && crt_tiles == o.crt_tiles && crt_persistent == o.crt_persistent &&
-               row_rows == o.row_rows && row_local == o.row_local && group == o.group && row_pass == o.row_pass;
+               row_rows == o.row_rows && row_local == o.row_local && group == o.group && row_pass == o.row_pass &&
+               encode_scalar == o.encode_scalar;
     }
 };
 
@@ -41,6 +42,7 @@ void apply(Context& ctx, const Settings& s) {
     t.row_rows = s.row_rows;
     t.row_local = s.row_local;
     t.row_pass = s.row_pass;
+    t.encode_scalar = s.encode_scalar;
     ctx.set_tuning(t);
     ctx.set_group(s.group);
 }
@@ -56,7 +58,8 @@ bool cached_autotune(int device, uint32_t N, uint32_t W, uint32_t L, AutotuneRep
 }
 
 void apply_autotune(Context& ctx, const AutotuneReport& r) {
-    apply(ctx, Settings{r.row_bits, r.crt_tiles, r.crt_persistent, r.row_rows, r.row_local, r.group, r.row_pass});
+    apply(ctx, Settings{r.row_bits, r.crt_tiles, r.crt_persistent, r.row_rows, r.row_local, r.group, r.row_pass,
+                        r.encode_scalar});
 }
 
 AutotuneReport autotune(Context& ctx, uint32_t max_group) {
@@ -115,7 +118,8 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
 
     AutotuneReport r{};
     Settings cur{g0.r_bits, ctx.tuning().crt_tiles, ctx.tuning().crt_persistent, ctx.tuning().row_rows,
-                 ctx.tuning().row_local, std::min(ctx.group(), gmax), ctx.tuning().row_pass};
+                 ctx.tuning().row_local, std::min(ctx.group(), gmax), ctx.tuning().row_pass,
+                 ctx.tuning().encode_scalar};
     double cur_us = measure(cur);
     r.us_per_product_default = cur_us;
     auto consider = [&](Settings s) {
@@ -128,7 +132,9 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
         }
         if (us < cur_us * 0.99) { cur = s; cur_us = us; }
     };
-    // Coordinate search: radix split, CRT tile shape, row-pass kernel and CTA, chain length.
+    // Coordinate search: encode kernel, radix split, CRT tile shape, row-pass kernel and CTA, chain length.
+    if (L <= kScalarMaxLimbs)
+        for (uint32_t es : {0u, 1u}) { Settings s = cur; s.encode_scalar = es; consider(s); }
     const uint32_t nb = g0.n_bits;
     for (uint32_t rb = (nb > 8 ? nb - 8 : 4); rb <= std::min<uint32_t>(8, nb); ++rb) {
         Settings s = cur; s.row_bits = rb; consider(s);
@@ -151,6 +157,7 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
     r.row_rows = cur.row_rows;
     r.row_local = cur.row_local;
     r.row_pass = cur.row_pass;
+    r.encode_scalar = cur.encode_scalar;
     r.group = cur.group;
     r.us_per_product_tuned = cur_us;
     r.candidates = candidates;

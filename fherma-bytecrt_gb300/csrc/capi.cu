@@ -132,6 +132,11 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
             bcg::Tuning t = c.tuning();
             t.row_pass = uint32_t(value);
             c.set_tuning(t);
+        } else if (k == "encode_scalar") {
+            require(value == 0 || value == 1, "encode_scalar must be 0 or 1");
+            bcg::Tuning t = c.tuning();
+            t.encode_scalar = uint32_t(value);
+            c.set_tuning(t);
         } else if (k == "wait_limit_ns") {
             require(value >= 0 && value <= 60000000000ll, "wait_limit_ns must be in [0, 6e10]");
             c.set_wait_limit_ns(uint64_t(value));
@@ -154,6 +159,7 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         else if (k == "crt_gap_fold") *value = c.tuning().crt_gap_fold;
         else if (k == "row_local") *value = c.tuning().row_local;
         else if (k == "row_pass") *value = c.tuning().row_pass;
+        else if (k == "encode_scalar") *value = c.tuning().encode_scalar;
         else if (k == "gap") *value = c.plan().gap;
         else if (k == "wait_limit_ns") *value = int64_t(c.wait_limit_ns());
         else throw std::invalid_argument("unknown tuning knob: " + k);
@@ -170,6 +176,7 @@ int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_repo
         out->crt_persistent = r.crt_persistent;
         out->row_local = r.row_local;
         out->row_pass = r.row_pass;
+        out->encode_scalar = r.encode_scalar;
         out->us_per_product_default = r.us_per_product_default;
         out->us_per_product_tuned = r.us_per_product_tuned;
     });
@@ -182,6 +189,16 @@ int bcg_multiply_sink(bcg_context* ctx, const uint32_t* a, const uint32_t* b, ui
         if (count == 0) return;
         require(a && b, "null buffer");
         ctx->ctx->multiply_host(a, b, nullptr, count, sink, user);
+    });
+}
+
+int bcg_multiply_dest(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t count, bcg_dest dest,
+                      void* user) {
+    return guarded([&] {
+        require(ctx && dest, "null argument");
+        if (count == 0) return;
+        require(a && b, "null buffer");
+        ctx->ctx->multiply_host(a, b, nullptr, count, nullptr, user, dest);
     });
 }
 

@@ -336,6 +336,7 @@ static cudaError_t launch_encode_t(EncodeArgs a, uint32_t nprod, cudaStream_t st
 }
 
 cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands) {
+    if (a.scalar) return launch_encode_scalar(a, nprod, st, operands);
     switch (a.L) {
         case 14: return launch_encode_t<14>(a, nprod, st, operands);
         case 28: return launch_encode_t<28>(a, nprod, st, operands);

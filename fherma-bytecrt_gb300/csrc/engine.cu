@@ -49,6 +49,7 @@ std::shared_ptr<const GeometryTables> geometry_tables(int device, const HostPlan
     upload(t->consts, plan.prime_consts.data(), plan.prime_consts.size() * 4);
     upload(t->tables, plan.ntt_tables.data(), plan.ntt_tables.size() * 4);
     upload(t->enc_b, plan.enc_b.data(), plan.enc_b.size() * 2);
+    upload(t->enc_pow, plan.enc_pow.data(), plan.enc_pow.size() * 4);
     cache[key] = t;
     return t;
 }
@@ -91,6 +92,7 @@ Context::Context(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, int devi
     bind_ntt();
 
     enc_.enc_b = geo_->enc_b.as<uint16_t>();
+    enc_.enc_pow = geo_->enc_pow.as<uint32_t>();
     for (uint32_t j = 0; j < g.P; ++j)
         enc_.prime[j] = make_uint2(plan_.prime_consts[4 * j], plan_.prime_consts[4 * j + 1]);
     enc_.N = g.N; enc_.L = g.L; enc_.P = g.P; enc_.K = g.enc_k; enc_.cols = g.enc_cols; enc_.chunks = g.enc_chunks;
@@ -161,6 +163,7 @@ void Context::set_row_bits(uint32_t row_bits) {
     plan_ = std::move(p);
     geo_ = std::move(geo);
     enc_.enc_b = geo_->enc_b.as<uint16_t>();
+    enc_.enc_pow = geo_->enc_pow.as<uint32_t>();
     bind_ntt();
 }
 
@@ -187,7 +190,11 @@ void Context::set_tuning(const Tuning& t) {
     if (t.row_rows > 4096) throw std::invalid_argument("row_rows must be at most 4096");
     if (t.row_local != 0 && t.row_local != 3 && t.row_local != 4) throw std::invalid_argument("row_local must be 0, 3 or 4");
     if (t.row_pass > 1) throw std::invalid_argument("row_pass must be 0 or 1");
+    if (t.encode_scalar > 1) throw std::invalid_argument("encode_scalar must be 0 or 1");
+    if (t.encode_scalar && plan_.g.L > kScalarMaxLimbs)
+        throw std::invalid_argument("encode_scalar needs L <= 32");
     tuning_ = t;
+    enc_.scalar = t.encode_scalar;
     ntt_.row_rows = t.row_rows;
     ntt_.row_local = t.row_local;
     ntt_.row_pass = t.row_pass;
@@ -406,47 +413,58 @@ bool is_pinned(const void* p) {
 }  // namespace
 
 namespace {
-// Page-locks [p, p + bytes) for one call if it is not pinned already (about
-// 3 ms per 1.8 GB on a GB300 host, unlocking 0.04 ms): the copy engine then
-// moves it asynchronously at the pinned rate, instead of a pageable copy call
-// that holds the host thread for its whole transfer.  Where locking fails
-// (memory already registered in part, or a system that refuses) the buffer
-// keeps the pageable path.
-class HostLock {
-public:
-    HostLock(const void* p, size_t bytes) {
-        if (!p || !bytes || is_pinned(p)) return;
-        if (cudaHostRegister(const_cast<void*>(p), bytes, cudaHostRegisterDefault) == cudaSuccess) ptr_ = p;
-        else cudaGetLastError();
+// Page locking of the caller's buffers for one call.  Only pages that lie
+// wholly inside a buffer are registered: registering an unaligned range locks
+// the whole pages around it, which would take in the neighbouring bytes of
+// other buffers (on the heap, one vector's last page is often the next one's
+// first), make their own registration fail, and turn any copy that starts in
+// such a page and runs past it into an invalid argument.  The partial pages at
+// either end of a buffer (less than a page each) travel through a small pinned
+// bounce buffer instead.  Registering 1.8 GB takes about 3 ms on a GB300 host,
+// unregistering 0.04 ms.
+struct HostSpan {
+    uintptr_t lo, hi;   // whole pages of [p, p + bytes): lo = page_up(p), hi = max(lo, page_down(p + bytes))
+    HostSpan(const void* p, size_t bytes, uintptr_t page) {
+        const uintptr_t b = uintptr_t(p), e = b + bytes;
+        lo = (b + page - 1) & ~(page - 1);
+        hi = std::max(lo, e & ~(page - 1));
     }
-    ~HostLock() { if (ptr_) cudaHostUnregister(const_cast<void*>(ptr_)); }
-    HostLock(const HostLock&) = delete;
-    HostLock& operator=(const HostLock&) = delete;
-private:
-    const void* ptr_ = nullptr;
 };
+
+uintptr_t page_size() {
+    static const uintptr_t page = uintptr_t(sysconf(_SC_PAGESIZE));
+    return page;
+}
+
+bool register_pages(uintptr_t lo, uintptr_t hi) {
+    if (hi <= lo) return true;
+    if (cudaHostRegister(reinterpret_cast<void*>(lo), size_t(hi - lo), cudaHostRegisterDefault) == cudaSuccess)
+        return true;
+    cudaGetLastError();
+    return false;
+}
 
 // Page-locks an input buffer one group at a time, just ahead of its copies,
 // so that locking overlaps the device's work on earlier groups instead of
 // preceding the call (2 x 1.8 GB took 6.1 ms up front).  Chunk k spans
-// [bound(k), bound(k + 1)) with page-aligned inner bounds, so neighbouring
-// chunks share no page; group k's bytes start in chunk k - 1 and end in
-// chunk k, and its copy is split where they meet.
+// [bound(k), bound(k + 1)): page-aligned bounds inside the buffer's whole
+// pages, bound(k) the first page boundary at or after group k's start, so
+// group k's bytes lie in chunks up to k (and in the partial pages at the
+// buffer's ends); its copy is cut where chunks meet.
 class ChunkLock {
 public:
     ChunkLock(const void* p, size_t total, size_t step, bool enable)
-        : base_(static_cast<const char*>(p)), total_(total), step_(step) {
+        : base_(static_cast<const char*>(p)), total_(total), step_(step), span_(p, total, page_size()) {
         if (!p || !total) return;
         pinned_ = is_pinned(p);
         if (pinned_ || !enable) return;
-        page_ = size_t(sysconf(_SC_PAGESIZE));
         chunks_ = (total + step - 1) / step;
-        regs_.assign(chunks_, nullptr);
+        regs_.assign(chunks_, false);
         active_ = true;
     }
     ~ChunkLock() {
-        for (const char* r : regs_)
-            if (r) cudaHostUnregister(const_cast<char*>(r));
+        for (size_t k = 0; k < chunks_; ++k)
+            if (regs_[k]) cudaHostUnregister(reinterpret_cast<void*>(bound(k)));
     }
     ChunkLock(const ChunkLock&) = delete;
     ChunkLock& operator=(const ChunkLock&) = delete;
@@ -454,42 +472,98 @@ public:
     void lock_through(size_t k) {
         if (!active_) return;
         for (; ok_ && next_ <= k && next_ < chunks_; ++next_) {
-            const char* lo = bound(next_);
-            const char* hi = bound(next_ + 1);
+            const uintptr_t lo = bound(next_), hi = bound(next_ + 1);
             if (hi <= lo) continue;
-            if (cudaHostRegister(const_cast<char*>(lo), size_t(hi - lo), cudaHostRegisterDefault) == cudaSuccess)
-                regs_[next_] = lo;
-            else {
-                cudaGetLastError();
-                ok_ = false;
-            }
+            if (register_pages(lo, hi)) regs_[next_] = true;
+            else ok_ = false;
         }
     }
+    // The buffer is pinned or being locked: its copies go through copy_to_device.
+    bool engaged() const { return pinned_ || active_; }
     // Group k's bytes may be copied asynchronously.
     bool usable(size_t k) const { return pinned_ || (active_ && ok_ && next_ > k); }
-    void copy_to_device(char* dst, size_t k, size_t bytes, cudaStream_t st) const {
+    // Copies group k: its pieces in locked chunks asynchronously, its pieces in
+    // the buffer's partial end pages through `bounce` (pinned, two pages: head,
+    // tail), and pieces in chunks that could not be locked as pageable copies
+    // (the call returns once they are read).
+    void copy_to_device(char* dst, size_t k, size_t bytes, cudaStream_t st, char* bounce) const {
         const char* src = base_ + k * step_;
         if (pinned_) {
             check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "input copy");
             return;
         }
-        const char* cut = std::min(bound(k), src + bytes);
-        if (cut > src) check(cudaMemcpyAsync(dst, src, size_t(cut - src), cudaMemcpyHostToDevice, st), "input copy");
-        if (src + bytes > cut)
-            check(cudaMemcpyAsync(dst + (cut - src), cut, size_t(src + bytes - cut), cudaMemcpyHostToDevice, st),
-                  "input copy");
+        const uintptr_t b = uintptr_t(src), e = b + bytes;
+        auto put = [&](uintptr_t x, uintptr_t y, const char* from) {
+            if (y > x) check(cudaMemcpyAsync(dst + (x - b), from, size_t(y - x), cudaMemcpyHostToDevice, st),
+                             "input copy");
+        };
+        // The bounce pages mirror the buffer's partial head and tail pages byte
+        // for byte, so groups that share one of them use disjoint bytes of it.
+        auto bounced = [&](uintptr_t x, uintptr_t y, char* mirror, uintptr_t origin) {
+            if (y <= x) return;
+            char* h = mirror + (x - origin);
+            std::memcpy(h, reinterpret_cast<const void*>(x), size_t(y - x));
+            put(x, y, h);
+        };
+        bounced(b, std::min(e, span_.lo), bounce, uintptr_t(base_));             // head page of the buffer
+        for (size_t j = 0; j < chunks_; ++j) {                      // whole pages, cut at chunk bounds
+            const uintptr_t x = std::max(b, uintptr_t(bound(j))), y = std::min(e, uintptr_t(bound(j + 1)));
+            put(x, y, reinterpret_cast<const char*>(x));
+        }
+        bounced(std::max(b, span_.hi), e, bounce + page_size(), span_.hi);       // tail page of the buffer
     }
 private:
-    const char* bound(size_t k) const {
-        if (k == 0) return base_;
-        if (k >= chunks_) return base_ + total_;
-        const uintptr_t x = (reinterpret_cast<uintptr_t>(base_ + k * step_) + page_ - 1) & ~uintptr_t(page_ - 1);
-        return std::min(reinterpret_cast<const char*>(x), base_ + total_);
+    uintptr_t bound(size_t k) const {
+        if (k == 0) return span_.lo;
+        if (k >= chunks_) return span_.hi;
+        const uintptr_t x = (uintptr_t(base_ + k * step_) + page_size() - 1) & ~(page_size() - 1);
+        return std::min(std::max(x, span_.lo), span_.hi);
     }
     const char* base_;
-    size_t total_, step_, page_ = 0, chunks_ = 0, next_ = 0;
+    size_t total_, step_;
+    HostSpan span_;
+    size_t chunks_ = 0, next_ = 0;
     bool pinned_ = false, active_ = false, ok_ = true;
-    std::vector<const char*> regs_;
+    std::vector<bool> regs_;
+};
+
+// Page-locks the output runs of one call as they are named (a caller's
+// destination, or the groups of a pageable output): each run's whole pages,
+// so neighbouring runs never share a registration.  prepare() says which part
+// the copy engine may write directly; the partial pages at either end of the
+// run come back through staging.
+class OutLock {
+public:
+    OutLock() = default;
+    ~OutLock() {
+        for (uintptr_t lo : regs_) cudaHostUnregister(reinterpret_cast<void*>(lo));
+    }
+    OutLock(const OutLock&) = delete;
+    OutLock& operator=(const OutLock&) = delete;
+    // [*lo, *hi): the bytes of [d, d + bytes) (offsets) that may be written
+    // directly; the rest, before and after, goes through staging.
+    void prepare(char* d, size_t bytes, size_t* lo, size_t* hi) {
+        const uintptr_t b = uintptr_t(d);
+        bool ours = false;
+        for (const auto& r : spans_) ours = ours || (b >= r.first && b < r.second);
+        if (!ours && is_pinned(d)) {   // memory the caller pinned itself (one allocation per run)
+            *lo = 0;
+            *hi = bytes;
+            return;
+        }
+        const HostSpan sp(d, bytes, page_size());
+        if (sp.hi > sp.lo && register_pages(sp.lo, sp.hi)) {
+            regs_.push_back(sp.lo);
+            spans_.push_back({sp.lo, sp.hi});
+            *lo = size_t(sp.lo - b);
+            *hi = size_t(sp.hi - b);
+        } else {
+            *lo = *hi = 0;
+        }
+    }
+private:
+    std::vector<uintptr_t> regs_;
+    std::vector<std::pair<uintptr_t, uintptr_t>> spans_;
 };
 }  // namespace
 
@@ -550,9 +624,11 @@ private:
 // into pinned staging.  A pinned output receives its products directly;
 // otherwise each group comes back into pinned staging with one copy, and the
 // output worker hands it, in order, to the sink (or copies it into c) while
-// the calling thread already issues the next groups.
+// the calling thread already issues the next groups.  A destination callback
+// names each group's output memory as the group is issued; the group is copied
+// straight into it where it can be page-locked, and through staging otherwise.
 void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, Sink sink,
-                            void* user) {
+                            void* user, Dest dest) {
     if (count == 0) return;
     const size_t cw = coeff_words();
     const size_t all = size_t(count) * cw * 4;
@@ -564,19 +640,22 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     const bool lock = count > 2 * g;
     ChunkLock lock_a(a, all, gbytes, lock), lock_b(b != a ? b : nullptr, all, gbytes, lock);
     ChunkLock& lock_b_or_a = b != a ? lock_b : lock_a;
-    HostLock lock_c(lock && !sink ? c : nullptr, all);
+    OutLock lock_out;
     // Leaving early (an error), no copy may still read or write the locked
     // buffers when they are unlocked: this guard is destroyed before them.
     struct Quiesce {
         cudaStream_t s0, s1, s2;
         ~Quiesce() { cudaStreamSynchronize(s0); cudaStreamSynchronize(s1); cudaStreamSynchronize(s2); }
     } quiesce{copy_in_, stream_, copy_out_};
-    const bool out_pinned = !sink && is_pinned(c);
+    const bool out_pinned = !sink && !dest && is_pinned(c);
     ensure_workspace(g);
     const uint32_t ngroups = (count + g - 1) / g;
     const uint32_t slots = std::min(kHostSlots, ngroups);
     constexpr size_t kPiece = size_t(4) << 20;
     ensure_host_slots(g, slots, !pageable_direct_ && !(is_pinned(a) && is_pinned(b)), !out_pinned);
+    if (edge_.bytes < 4 * page_size()) edge_.allocate(4 * page_size());
+    char* bounce_a = edge_.as<char>();
+    char* bounce_b = b != a ? bounce_a + 2 * page_size() : bounce_a;
     const size_t max_pieces = (size_t(g) * cw * 4 + kPiece - 1) / kPiece;
     for (uint32_t s = 0; s < slots; ++s)
         while (piece_ev_[s].size() < max_pieces) {
@@ -585,9 +664,9 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
             piece_ev_[s].push_back(e);
         }
     auto group_size = [&](uint32_t gi) { return std::min(g, count - gi * g); };
-    auto stage_in = [&](ChunkLock& lk, uint32_t gi, char* h, char* d, const char* x, size_t bytes) {
-        if (lk.usable(gi)) {                   // pinned or locked: asynchronous
-            lk.copy_to_device(d, gi, bytes, copy_in_);
+    auto stage_in = [&](ChunkLock& lk, uint32_t gi, char* h, char* d, const char* x, size_t bytes, char* bounce) {
+        if (lk.engaged()) {                    // pinned or locked: asynchronous
+            lk.copy_to_device(d, gi, bytes, copy_in_, bounce);
             return;
         }
         if (pageable_direct_) {                // read in place (holds this thread for the transfer)
@@ -611,7 +690,30 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     // come back in 4 MiB pieces that this thread hands over as each lands (one
     // product through the plugin: 0.71 ms through the worker, 0.5 ms so).
     const bool inline_out = !out_pinned && ngroups <= 2;
-    const bool worker_out = !out_pinned && !inline_out;
+    // Larger calls into a pageable output or a caller's destinations lock each
+    // group's run of the output as it is issued and copy straight into it.
+    const bool run_out = !out_pinned && !inline_out && !sink;
+    const bool worker_out = !out_pinned && !inline_out && sink;
+    // The parts of a run that are not locked (its partial end pages, or all
+    // of it where locking fails) come back through the slot's staging; the
+    // calling thread moves them before the slot's staging is reused and at
+    // the end.
+    struct Staged { char* dst = nullptr; size_t lo = 0, hi = 0, bytes = 0; } staged[kHostSlots];
+    auto settle_staged = [&](uint32_t s) {
+        Staged& st = staged[s];
+        if (!st.dst) return;
+        check(cudaEventSynchronize(ev_host_[s]), "output copy");
+        const char* h = reinterpret_cast<const char*>(io_out_[s].as<uint32_t>());
+        parallel_copy(st.dst, h, st.lo);
+        parallel_copy(st.dst + st.hi, h + st.hi, st.bytes - st.hi);
+        st.dst = nullptr;
+    };
+    auto named = [&](uint32_t gi, size_t words) {
+        if (!dest) return reinterpret_cast<char*>(c + size_t(gi) * g * cw);
+        uint32_t* p = dest(user, words);
+        if (!p) throw std::invalid_argument("the output destination callback returned no memory");
+        return reinterpret_cast<char*>(p);
+    };
     if (worker_out) {
         if (!worker_) worker_ = std::make_unique<HostWorker>();
         worker_->post([&] {
@@ -673,13 +775,13 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         if (gi >= slots) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
         // Operand A first: the device encodes it while operand B comes in.
         stage_in(lock_a, gi, reinterpret_cast<char*>(h), reinterpret_cast<char*>(d),
-                 reinterpret_cast<const char*>(a + off), bytes);
+                 reinterpret_cast<const char*>(a + off), bytes, bounce_a);
         check(cudaEventRecord(ev_in_[s], copy_in_), "event");
         check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
         if (gi >= slots) check(cudaStreamWaitEvent(stream_, ev_out_[s], 0), "slot reuse");
         chain(d, d + g * cw, d + 2 * g * cw, n, ws_.as<uint32_t>(), stream_, nullptr, [&] {
             stage_in(lock_b_or_a, gi, reinterpret_cast<char*>(h ? h + g * cw : nullptr),
-                     reinterpret_cast<char*>(d + g * cw), reinterpret_cast<const char*>(b + off), bytes);
+                     reinterpret_cast<char*>(d + g * cw), reinterpret_cast<const char*>(b + off), bytes, bounce_b);
             check(cudaEventRecord(ev_in_[s], copy_in_), "event");
             check(cudaStreamWaitEvent(stream_, ev_in_[s], 0), "event wait");
         });
@@ -692,6 +794,23 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
                 check(cudaMemcpyAsync(hs + po, ds + po, std::min(kPiece, bytes - po), cudaMemcpyDeviceToHost,
                                       copy_out_), "output copy");
                 check(cudaEventRecord(piece_ev_[s][k], copy_out_), "event");
+            }
+        } else if (run_out) {
+            settle_staged(s);
+            char* dst = named(gi, bytes / 4);
+            const char* ds = reinterpret_cast<const char*>(d + 2 * g * cw);
+            char* hs = reinterpret_cast<char*>(io_out_[s].as<uint32_t>());
+            size_t lo = 0, hi = 0;
+            lock_out.prepare(dst, bytes, &lo, &hi);
+            if (hi > lo)
+                check(cudaMemcpyAsync(dst + lo, ds + lo, hi - lo, cudaMemcpyDeviceToHost, copy_out_), "output copy");
+            if (lo > 0 || hi < bytes) {
+                if (lo > 0) check(cudaMemcpyAsync(hs, ds, lo, cudaMemcpyDeviceToHost, copy_out_), "output copy");
+                if (hi < bytes)
+                    check(cudaMemcpyAsync(hs + hi, ds + hi, bytes - hi, cudaMemcpyDeviceToHost, copy_out_),
+                          "output copy");
+                check(cudaEventRecord(ev_host_[s], copy_out_), "event");
+                staged[s] = Staged{dst, lo, hi, bytes};
             }
         } else {
             check(cudaMemcpyAsync(out_pinned ? c + off : io_out_[s].as<uint32_t>(), d + 2 * g * cw, bytes,
@@ -712,7 +831,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
             const uint32_t s = gi % slots;
             const size_t bytes = size_t(group_size(gi)) * cw * 4;
             const char* src = reinterpret_cast<const char*>(io_out_[s].as<uint32_t>());
-            char* dst = reinterpret_cast<char*>(c + size_t(gi) * g * cw);
+            char* dst = named(gi, bytes / 4);
             if (sink) sink(user, nullptr, bytes / 4);
             for (size_t k = 0, po = 0; po < bytes; ++k, po += kPiece) {
                 const size_t pn = std::min(kPiece, bytes - po);
@@ -729,6 +848,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         if (out_error) std::rethrow_exception(out_error);
     } else {
         check(cudaStreamSynchronize(copy_out_), "output copy");
+        for (uint32_t s = 0; s < slots; ++s) settle_staged(s);
     }
     check_status();
 }

@@ -83,7 +83,7 @@ struct PinnedBuffer {
 // Every Context of the same geometry on a device shares one copy (moduli of a
 // geometry differ only in the CRT weights and q, which stay per Context).
 struct GeometryTables {
-    DeviceBuffer consts, tables, enc_b;
+    DeviceBuffer consts, tables, enc_b, enc_pow;
 };
 std::shared_ptr<const GeometryTables> geometry_tables(int device, const HostPlan& plan);
 
@@ -135,10 +135,13 @@ public:
     // Whole products.
     void multiply_device(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, cudaStream_t st);
     // Host buffers.  With a sink, c is unused: the product goes to
-    // sink(user, words, n) in order, one staged piece at a time.
+    // sink(user, words, n) in order, one staged piece at a time.  With a
+    // destination, c is unused too: dest(user, n) names, in order, where each
+    // run of n words goes, and the library copies the run there.
     using Sink = void (*)(void* user, const uint32_t* words, size_t n);
+    using Dest = uint32_t* (*)(void* user, size_t n);
     void multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count,
-                       Sink sink = nullptr, void* user = nullptr);
+                       Sink sink = nullptr, void* user = nullptr, Dest dest = nullptr);
 
     // Throws DeviceTimeout (after clearing it) if a kernel reported a wait timeout.
     void synchronize(cudaStream_t st);
@@ -208,6 +211,7 @@ private:
     static constexpr uint32_t kHostSlots = 6;
     DeviceBuffer io_dev_[kHostSlots];
     PinnedBuffer io_in_[kHostSlots], io_out_[kHostSlots];
+    PinnedBuffer edge_;   // partial end pages of the operands (two pages per operand)
     cudaEvent_t ev_in_[kHostSlots] = {}, ev_done_[kHostSlots] = {}, ev_out_[kHostSlots] = {};
     cudaEvent_t ev_host_[kHostSlots] = {};   // staged output landed (waited on by the output worker only)
     std::vector<cudaEvent_t> piece_ev_[kHostSlots];   // 4 MiB output pieces of small calls
@@ -222,7 +226,7 @@ private:
 // the fastest and records it for later Contexts of the same geometry.
 struct AutotuneReport {
     uint32_t group = 0, crt_tiles = 0, crt_persistent = 0, row_rows = 0, row_local = 0, row_bits = 0, candidates = 0;
-    uint32_t row_pass = 0;
+    uint32_t row_pass = 0, encode_scalar = 0;
     double us_per_product_default = 0, us_per_product_tuned = 0;
 };
 AutotuneReport autotune(Context& ctx, uint32_t max_group);

@@ -11,6 +11,7 @@ namespace bcg {
 
 constexpr uint32_t kMaxPrimes = 256;
 constexpr uint32_t kMaxLimbs = 64;
+constexpr uint32_t kScalarMaxLimbs = 32;   // the CUDA-core encoder (encode_scalar.cu) takes L <= 32
 
 // Kernel arguments are passed by value; the small per-point constants ride in
 // the parameter space (constant bank), where warp-uniform reads are free.
@@ -22,6 +23,8 @@ struct EncodeArgs {
     uint32_t* out1;
     size_t out_stride;
     const uint16_t* enc_b;   // fp16 byte-power matrix, chunked
+    const uint32_t* enc_pow; // [P][2L] 2^(16m) * 2^32 mod p_j (the CUDA-core encoder's half-limb weights)
+    uint32_t scalar;         // 1: CUDA-core encoder (L <= 32), 0: tcgen05 encoder
     uint32_t N, L, P, K, cols, chunks;
     uint32_t* status;
     uint64_t wait_limit_ns;  // limit of waits on other roles (the context's wait limit)
@@ -59,14 +62,18 @@ struct Tuning {
     uint32_t row_local = 0;      // row pass elements per thread: 0 default, 3 (8 elements) or 4 (16, R = 256)
     uint32_t row_pass = 0;       // row pass kernel: 0 row_kernel, 1 row_sliced_kernel (per-row twist tables
                                  // shared by the products of a CTA's slice); an autotuner candidate
+    uint32_t encode_scalar = 0;  // encode kernel: 0 tcgen05 digit GEMM, 1 CUDA-core Montgomery (L <= 32)
 };
 
 size_t encode_smem_bytes(uint32_t K, uint32_t group_cols);
 uint32_t encode_group_cols(uint32_t cols, uint32_t K);
 size_t crt_smem_bytes(uint32_t NC, uint32_t tiles);
 
-// Encodes operand A (and operand B when operands == 2) of nprod products (grid.y = operand).
+// Encodes operand A (and operand B when operands == 2) of nprod products (grid.y = operand);
+// a.scalar selects the CUDA-core encoder.
 cudaError_t launch_encode(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands = 2);
+// CUDA-core encoder (encode_scalar.cu): same residues, canonical in [0, p).
+cudaError_t launch_encode_scalar(const EncodeArgs& a, uint32_t nprod, cudaStream_t st, uint32_t operands);
 cudaError_t launch_crt(const CrtArgs& a, uint32_t nprod, cudaStream_t st, uint32_t tiles = 2);
 // Persistent warp-specialised CRT (crt_persistent.cu): same results, overlapped epilogue.
 cudaError_t launch_crt_persistent(const CrtArgs& a, uint32_t nprod, cudaStream_t st);

@@ -373,6 +373,18 @@ HostPlan make_plan(uint32_t N, uint32_t W, uint32_t L, const uint32_t* qw, uint3
         dst[kmajor_offset(n, 4 * L, g.enc_k) / 2] = half_bits(dg[d]);
     }
 
+    // CUDA-core encoder powers: half-limb m (16 bits) weighs 2^(16m) * R mod p_j
+    // (R = 2^32), so one Montgomery reduction of the weighted sum is x mod p_j.
+    plan.enc_pow.assign(size_t(g.P) * 2 * L, 0);
+    for (uint32_t j = 0; j < g.P; ++j) {
+        const uint32_t pj = plan.primes[j];
+        uint64_t w = pow_mod(2, 32, pj);
+        for (uint32_t m = 0; m < 2 * L; ++m) {
+            plan.enc_pow[size_t(j) * 2 * L + m] = uint32_t(w);
+            w = w * 65536 % pj;
+        }
+    }
+
     // CRT B: K chunk kc holds k = 4u + a for terms u in [16kc, 16kc + 16), rows
     // (MMA N) e < crt_n.  Entry = digit e of (256^a * weight_u) mod q.
     plan.crt_b.assign(size_t(g.crt_kchunks) * kCrtChunkK * g.crt_n, 0);

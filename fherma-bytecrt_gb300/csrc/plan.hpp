@@ -39,6 +39,7 @@ struct HostPlan {
                                            // N^-1 * inv(Prod/p) * 2^32 mod p
     std::vector<uint32_t> ntt_tables;      // P x table_stride x (value, Shoup companion)
     std::vector<uint16_t> enc_b;           // fp16 bit patterns, chunked core-matrix order
+    std::vector<uint32_t> enc_pow;         // [P][2L]: 2^(16m) * 2^32 mod p_j (CUDA-core encoder)
     std::vector<uint16_t> crt_b;           // fp16 bit patterns, chunked core-matrix order
     std::vector<float> invp;               // float(1.0 / p_j)
     double q_inv_scaled = 0;               // 2^(32*(L-T)) / q, T = min(L, 3)

@@ -25,6 +25,7 @@ BCG_ERR_TIMEOUT = 6
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 SINK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.c_size_t)
+DEST = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t)
 
 
 class BcgError(RuntimeError):
@@ -48,6 +49,7 @@ class bcg_autotune_report(ctypes.Structure):
     _fields_ = [("group", ctypes.c_uint32), ("crt_tiles", ctypes.c_uint32), ("row_rows", ctypes.c_uint32),
                 ("row_bits", ctypes.c_uint32), ("candidates", ctypes.c_uint32), ("crt_persistent", ctypes.c_uint32),
                 ("row_local", ctypes.c_uint32), ("row_pass", ctypes.c_uint32),
+                ("encode_scalar", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
                 ("us_per_product_default", ctypes.c_double), ("us_per_product_tuned", ctypes.c_double)]
 
 
@@ -101,6 +103,7 @@ def lib():
         L.bcg_context_get_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.bcg_multiply.argtypes = [vp, _u32p, _u32p, _u32p, ctypes.c_uint32]
         L.bcg_multiply_sink.argtypes = [vp, _u32p, _u32p, ctypes.c_uint32, SINK, vp]
+        L.bcg_multiply_dest.argtypes = [vp, _u32p, _u32p, ctypes.c_uint32, DEST, vp]
         L.bcg_context_autotune.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(bcg_autotune_report)]
         L.bcg_multiply_device.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
         L.bcg_multiply_device_static.argtypes = [vp, vp, vp, vp, ctypes.c_uint32, vp]
@@ -272,6 +275,32 @@ class Multiplier:
         _check(lib().bcg_multiply_sink(self._h, _p(a), _p(b), count, cb, None))
         if errors:
             raise errors[0]
+
+    def multiply_dest(self, a: np.ndarray, b: np.ndarray, dest) -> None:
+        """c = a*b from host buffers into memory the caller names run by run:
+        dest(n) returns the host address (an int) where the next n words go,
+        or 0 to refuse (BcgError).  The memory must stay valid and untouched
+        until the call returns."""
+        a = np.ascontiguousarray(a, dtype=np.uint32)
+        b = np.ascontiguousarray(b, dtype=np.uint32)
+        if a.shape != b.shape or a.size % (self.N * self.L):
+            raise ValueError("operands must be [count][N][L] uint32 of equal shape")
+        count = a.size // (self.N * self.L)
+        errors = []
+
+        def call(user, n):
+            try:
+                return int(dest(int(n)) or 0) or None
+            except BaseException as e:   # never raise through the C ABI
+                errors.append(e)
+                return None
+
+        cb = DEST(call)
+        try:
+            _check(lib().bcg_multiply_dest(self._h, _p(a), _p(b), count, cb, None))
+        finally:
+            if errors:
+                raise errors[0]
 
     def multiply_into(self, a, b, c, count: int):
         """Host buffers given as addresses (e.g. pinned torch tensors): c = a*b, synchronous."""

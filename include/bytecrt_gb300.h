@@ -98,6 +98,10 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *                table products; 1: the sliced row pass, whose CTAs build each
  *                row's twist and untwist factors once and share them with every
  *                product of their slice (one product per twist)
+ *   "encode_scalar"  0 (default): the encode is an exact fp16 digit GEMM on
+ *                the tensor cores; 1: a CUDA-core encoder with one Montgomery
+ *                product per limb and prime (the reference's scalar encoder,
+ *                native-smoke/rns-encode.cuh:30-77), for L <= 32 only
  *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
  *                Re-plans the twiddle and twist tables (the primes stay).
  *   "wait_limit_ns"  limit of a kernel's wait on another warp role's arrival,
@@ -114,8 +118,9 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *                bounded device waits. */
 int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value);
 int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* value);
-/* Autotuner: times whole launch chains on synthetic operands for every value
- * of row_bits, then the CRT kernel and tile shape, row_local, row_pass, row_rows and group (coordinate search, at most
+/* Autotuner: times whole launch chains on synthetic operands for both encode
+ * kernels (L <= 32), every value of row_bits, then the CRT kernel and tile
+ * shape, row_local, row_pass, row_rows and group (coordinate search, at most
  * max_group products per chain and 4 GB of workspace), keeps the fastest, and
  * records it so that contexts of the same geometry created later in the
  * process (including those of bcg_batch and bcg_server) start from it.  The
@@ -125,6 +130,8 @@ typedef struct bcg_autotune_report {
     uint32_t candidates;    /* settings timed */
     uint32_t crt_persistent;
     uint32_t row_local, row_pass;
+    uint32_t encode_scalar;
+    uint32_t reserved;
     double us_per_product_default, us_per_product_tuned;
 } bcg_autotune_report;
 int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_report* out);
@@ -147,6 +154,21 @@ int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_
  * No counterpart in the reference. */
 typedef void (*bcg_sink)(void* user, const uint32_t* words, size_t n);
 int bcg_multiply_sink(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t count, bcg_sink sink,
+                      void* user);
+/* Like bcg_multiply, but the caller names the output memory run by run: the
+ * product ([count][N][L] words) travels in groups, and for each group, in
+ * order, dest(user, n) is called on the calling thread with the group's word
+ * count n and returns where those n words go (host memory that the caller
+ * neither reads nor writes until the call returns; NULL fails the call with
+ * BCG_ERR_INVALID).  Every run is named before any of its words is written.
+ * The library page-locks each run as it is named (runs that follow one
+ * another in one buffer share their boundary pages) and copies the product
+ * straight into it; what cannot be locked comes back through pinned staging.
+ * For callers that grow their own output run by run while earlier groups
+ * compute (the plugin's owned std::vector: its zero fill overlaps the device
+ * work instead of a staging copy after it).  No counterpart in the reference. */
+typedef uint32_t* (*bcg_dest)(void* user, size_t n);
+int bcg_multiply_dest(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t count, bcg_dest dest,
                       void* user);
 /* device buffers, asynchronous on `stream` */
 int bcg_multiply_device(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c,

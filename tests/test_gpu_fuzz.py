@@ -52,7 +52,8 @@ def test_random_points_bit_exact(case):
     n_bits = N.bit_length() - 1
     knobs = {"crt_persistent": int(rng.integers(2)), "crt_tiles": int(rng.integers(1, 3)),
              "row_rows": int(rng.choice([0, 8, 64])), "crt_gap_fold": int(rng.integers(2)),
-             "row_local": int(rng.choice([0, 3])), "row_pass": int(rng.integers(2))}
+             "row_local": int(rng.choice([0, 3])), "row_pass": int(rng.integers(2)),
+             "encode_scalar": int(rng.integers(2)) if len(q) <= 32 else 0}
     splits = [rb for rb in range(max(4, n_bits - 8), min(8, n_bits) + 1) if not (N >> rb > 1 and rb < 5)]
     knobs["row_bits"] = int(rng.choice(splits))
     for k, v in knobs.items():

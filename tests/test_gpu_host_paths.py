@@ -112,3 +112,83 @@ def test_sink_exception_is_reraised():
     # The context stays usable.
     assert np.array_equal(m.multiply(a, b), device_products(m, a, b))
     m.close()
+
+
+@pytest.mark.parametrize("N,W,count", CASES)
+def test_dest_runs_fill_one_buffer(N, W, count):
+    """bcg_multiply_dest as the plugin drives it: consecutive runs of one
+    pageable buffer (neighbouring runs share pages), named in order."""
+    pkg = package()
+    q = pkg.inputs.modulus(W, 35)
+    m = pkg.Multiplier(N, W, q)
+    a, b = operands(pkg, q, N, count, 500)
+    out = np.zeros(a.size + 7, dtype=np.uint32)[3:3 + a.size]     # not page-aligned
+    sizes = []
+
+    def dest(n):
+        at = sum(sizes)
+        sizes.append(n)
+        return out.ctypes.data + 4 * at
+
+    m.multiply_dest(a, b, dest)
+    assert sum(sizes) == a.size and all(n > 0 for n in sizes)
+    assert np.array_equal(out.reshape(a.shape), device_products(m, a, b))
+    m.close()
+
+
+@pytest.mark.parametrize("layout", ["separate", "reversed", "pinned"])
+def test_dest_layouts(layout):
+    """Runs in separate buffers, runs placed back to front in one buffer (each
+    run's last page is locked already: its tail comes back through staging),
+    and runs in pinned memory: the same products as the device path."""
+    pkg = package()
+    N, W, count = 65536, 1747, 10
+    q = pkg.inputs.modulus(W, 36)
+    m = pkg.Multiplier(N, W, q)
+    a, b = operands(pkg, q, N, count, 600)
+    words = a.size
+    keep, runs = [], []
+    whole = (torch.zeros(words, dtype=torch.int32).pin_memory() if layout == "pinned"
+             else np.zeros(words + 5, dtype=np.uint32)[1:1 + words])
+    base = whole.data_ptr() if layout == "pinned" else whole.ctypes.data
+    placed = [0]
+
+    def dest(n):
+        if layout == "separate":
+            buf = np.zeros(n + 3, dtype=np.uint32)[2:2 + n]
+            keep.append(buf)
+            runs.append(buf)
+            return buf.ctypes.data
+        placed[0] += n
+        start = words - placed[0] if layout == "reversed" else placed[0] - n
+        runs.append((start, n))
+        return base + 4 * start
+
+    m.multiply_dest(a, b, dest)
+    if layout == "separate":
+        got = np.concatenate(runs)
+    else:
+        flat = whole.numpy().view(np.uint32) if layout == "pinned" else whole
+        got = np.concatenate([flat[s:s + n] for s, n in runs])
+    assert np.array_equal(got.reshape(a.shape), device_products(m, a, b))
+    m.close()
+
+
+def test_dest_refusal_fails_the_call_and_keeps_the_context():
+    pkg = package()
+    N, W, count = 65536, 1747, 9
+    q = pkg.inputs.modulus(W, 37)
+    m = pkg.Multiplier(N, W, q)
+    a, b = operands(pkg, q, N, count, 700)
+    out = np.zeros(a.size, dtype=np.uint32)
+    named = []
+
+    def dest(n):
+        named.append(n)
+        return 0 if len(named) == 2 else out.ctypes.data + 4 * sum(named[:-1])
+
+    with pytest.raises(pkg.BcgError):
+        m.multiply_dest(a, b, dest)
+    assert len(named) == 2
+    assert np.array_equal(m.multiply(a, b), device_products(m, a, b))
+    m.close()

@@ -56,6 +56,50 @@ def test_encode_matches_oracle(N, W):
         assert np.array_equal(got % p, o.encode(x).astype(np.uint64))
 
 
+SCALAR = [(16, 40), (64, 100), (256, 434), (2048, 300), (1024, 1020), (16384, 434), (32768, 868)]
+
+
+@pytest.mark.parametrize("N,W", SCALAR)
+def test_encode_scalar_matches_oracle(N, W):
+    """The CUDA-core encoder (L <= 32) leaves canonical residues equal to the
+    oracle's, for canonical operands and for limbs at their 32-bit maximum, and
+    whole products through it stay bit-exact."""
+    pkg = package()
+    q = pkg.inputs.modulus(W, 41)
+    m, o = pkg.Multiplier(N, W, q), O.Oracle(N, W, q)
+    m.set_tuning("encode_scalar", 1)
+    assert m.get_tuning("encode_scalar") == 1
+    L = len(q)
+    ones = np.full((N, L), 0xFFFFFFFF, dtype=np.uint32)
+    cases = [pkg.inputs.uniform(q, N, 12), pkg.inputs.fixture(q, N, "minus_one"), ones]
+    pw = m.plane_words
+    for x, y in ((cases[0], cases[1]), (cases[2], cases[0])):
+        pa, pb = empty(pw), empty(pw)
+        m.encode_device(dev(x), dev(y), pa, pb, pw, 1)
+        m.synchronize()
+        for z, planes in ((x, pa), (y, pb)):
+            assert np.array_equal(host(planes).reshape(o.P, N), o.encode(z))
+    # Three products per chain: the grid walks products and operands.
+    a = np.stack([pkg.inputs.uniform(q, N, 90 + i) for i in range(3)])
+    b = np.stack([pkg.inputs.fixture(q, N, "half_high"), pkg.inputs.uniform(q, N, 95),
+                  pkg.inputs.fixture(q, N, "minus_one")])
+    out = torch.zeros((3, N, L), dtype=torch.int32, device="cuda")
+    m.multiply_device(dev(a), dev(b), out, 3)
+    m.synchronize()
+    for i in range(3):
+        assert np.array_equal(host(out[i]), o.multiply(a[i], b[i])), i
+    m.set_tuning("encode_scalar", 0)
+    m.close()
+
+
+def test_encode_scalar_rejects_wide_points():
+    pkg = package()
+    m, _, _ = setup(65536, 1747, 1)
+    with pytest.raises(Exception, match="L <= 32"):
+        m.set_tuning("encode_scalar", 1)
+    assert m.get_tuning("encode_scalar") == 0
+
+
 @pytest.mark.parametrize("N,W", SMALL + FULL)
 def test_negacyclic_terms_match_oracle(N, W):
     pkg = package()
@@ -249,14 +293,16 @@ def test_autotune_applies_and_is_remembered():
     assert r["candidates"] >= 5
     assert 0 < r["us_per_product_tuned"] <= r["us_per_product_default"] * 1.05
     assert r["crt_tiles"] in (1, 2) and 1 <= r["group"] <= 8
-    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits", "row_pass"):
+    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits", "row_pass",
+                 "encode_scalar"):
         assert m.get_tuning(knob) == r[knob], knob
     a, b = pkg.inputs.uniform(q, N, 3), pkg.inputs.uniform(q, N, 4)
     assert np.array_equal(m.multiply(a, b), O.Oracle(N, W, q).multiply(a, b))
     # Another context of the same geometry (another q) starts from the tuned shapes.
     q2 = pkg.inputs.modulus(W, 32)
     m2 = pkg.Multiplier(N, W, q2)
-    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits", "row_pass"):
+    for knob in ("group", "crt_tiles", "crt_persistent", "row_rows", "row_local", "row_bits", "row_pass",
+                 "encode_scalar"):
         assert m2.get_tuning(knob) == r[knob], knob
     a2, b2 = pkg.inputs.uniform(q2, N, 5), pkg.inputs.uniform(q2, N, 6)
     assert np.array_equal(m2.multiply(a2, b2), O.Oracle(N, W, q2).multiply(a2, b2))

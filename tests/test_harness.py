@@ -108,3 +108,29 @@ def test_batched_harness_bit_exact(tmp_path):
         got = np.fromfile(tmp_path / "out" / f"{i:06d}" / "c.bin", dtype="<u4").reshape(B, N, len(q))
         for k in range(B):
             assert np.array_equal(got[k], o.multiply(a[k], b[k]))
+
+
+@pytest.mark.gpu
+def test_batched_harness_large_output_bit_exact(tmp_path):
+    """A batched case whose owned output is above 128 MiB takes the shim's
+    destination path (the vector grows run by run and each group is copied
+    straight into it): every product equals the device-resident one, and two
+    of them the oracle."""
+    pkg = package()
+    N, W, B = 65536, 1747, 10
+    q = pkg.inputs.modulus(W, 5)
+    a = np.stack([pkg.inputs.uniform(q, N, 40 + k) for k in range(B)])
+    b = np.stack([pkg.inputs.uniform(q, N, 60 + k) for k in range(B)])
+    assert a.nbytes >= 128 << 20
+    write_point(str(tmp_path), N, W, q, [(a, b)], B=B)
+    r = subprocess.run([binary("solution_batched"), str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    res = json.load(open(tmp_path / "out" / "results.json"))
+    assert [c["status"] for c in res["cases"]] == ["ok"]
+    got = np.fromfile(tmp_path / "out" / "000000" / "c.bin", dtype="<u4").reshape(B, N, len(q))
+    m = pkg.Multiplier(N, W, q)
+    assert np.array_equal(got, m.multiply(a, b))
+    m.close()
+    o = O.Oracle(N, W, q)
+    for k in (0, B - 1):
+        assert np.array_equal(got[k], o.multiply(a[k], b[k])), k
