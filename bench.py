@@ -483,8 +483,11 @@ def run_native(args):
     link_before = host_link(a_h, a_dev, c_h, c_dev)
     barrier()
     t0 = time.perf_counter()
+    e2e_steps = []
     for _ in range(args.steps):
+        ts = time.perf_counter()
         m.multiply_into(a_h, b_h, c_h, B)
+        e2e_steps.append(1000.0 * (time.perf_counter() - ts))
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     barrier()
     e2e_value = world * B * args.steps / e2e_s
@@ -568,6 +571,8 @@ def run_native(args):
                 "link_bound": link_bound(link, 2 * N * L * 4, N * L * 4),
                 "link_frac": e2e_value / world / link_bound(link, 2 * N * L * 4, N * L * 4),
                 "link_model_even_split": link_model_even_split(link, 2 * N * L * 4, N * L * 4),
+                "step_ms": {"min": min(e2e_steps), "median": sorted(e2e_steps)[len(e2e_steps) // 2],
+                            "max": max(e2e_steps)},
                 "host_link": link},
         "stream_launch": {"products_per_s": stream_value, "ms_per_step": stream_ms / max(3, args.steps // 2)},
         "plain": {"device_ms_per_product": plain_ms, "device_products_per_s": 1000.0 / plain_ms,

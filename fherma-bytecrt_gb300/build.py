@@ -74,10 +74,14 @@ def build(verbose: bool = False) -> str:
     harness_src = os.path.join(CSRC, "harness.cpp")
     for suffix, defs in (("", []), ("_batched", ["-DFHERMA_BATCHED"])):
         shim = os.path.join(HERE, f"libfherma_gb300{suffix}.so")
-        if _stale(shim, [shim_src, LIB, *_headers()]):
+        if _stale(shim, [shim_src, LIB, os.path.abspath(__file__), *_headers()]):
             tmp = shim + f".tmp{os.getpid()}"
-            subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-Wl,--wrap=memcpy",
-                            "-Wl,--wrap=memmove", "-Wl,--wrap=memset", *defs, *inc, "-o", tmp, shim_src,
+            # The shim's own references (the owned vector's growth and copies, which the wraps
+            # below make parallel) bind to its own definitions: a host executable's instantiation
+            # of the same std::vector members, built without the wraps, must not replace them.
+            subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-fvisibility-inlines-hidden",
+                            "-Wl,-Bsymbolic-functions", "-Wl,--wrap=memcpy", "-Wl,--wrap=memmove",
+                            "-Wl,--wrap=memset", *defs, *inc, "-o", tmp, shim_src,
                             "-L", HERE, "-lbytecrt_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
             os.replace(tmp, shim)
         harness = os.path.join(HERE, f"solution{suffix}")
