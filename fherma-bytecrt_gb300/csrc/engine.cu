@@ -1,5 +1,6 @@
 // Host engine: device tables, workspace and the launch chain (see engine.hpp).
 #include "engine.hpp"
+#include "host_pages.hpp"
 
 #include <algorithm>
 #include <cstring>
@@ -414,23 +415,10 @@ bool is_pinned(const void* p) {
 
 namespace {
 // Page locking of the caller's buffers for one call.  Only pages that lie
-// wholly inside a buffer are registered: registering an unaligned range locks
-// the whole pages around it, which would take in the neighbouring bytes of
-// other buffers (on the heap, one vector's last page is often the next one's
-// first), make their own registration fail, and turn any copy that starts in
-// such a page and runs past it into an invalid argument.  The partial pages at
-// either end of a buffer (less than a page each) travel through a small pinned
-// bounce buffer instead.  Registering 1.8 GB takes about 3 ms on a GB300 host,
-// unregistering 0.04 ms.
-struct HostSpan {
-    uintptr_t lo, hi;   // whole pages of [p, p + bytes): lo = page_up(p), hi = max(lo, page_down(p + bytes))
-    HostSpan(const void* p, size_t bytes, uintptr_t page) {
-        const uintptr_t b = uintptr_t(p), e = b + bytes;
-        lo = (b + page - 1) & ~(page - 1);
-        hi = std::max(lo, e & ~(page - 1));
-    }
-};
-
+// wholly inside a buffer are registered (host_pages.hpp says why); the
+// partial pages at either end of a buffer (less than a page each) travel
+// through a small pinned bounce buffer instead.  Registering 1.8 GB takes
+// about 3 ms on a GB300 host, unregistering 0.04 ms.
 uintptr_t page_size() {
     static const uintptr_t page = uintptr_t(sysconf(_SC_PAGESIZE));
     return page;
@@ -446,33 +434,29 @@ bool register_pages(uintptr_t lo, uintptr_t hi) {
 
 // Page-locks an input buffer one group at a time, just ahead of its copies,
 // so that locking overlaps the device's work on earlier groups instead of
-// preceding the call (2 x 1.8 GB took 6.1 ms up front).  Chunk k spans
-// [bound(k), bound(k + 1)): page-aligned bounds inside the buffer's whole
-// pages, bound(k) the first page boundary at or after group k's start, so
-// group k's bytes lie in chunks up to k (and in the partial pages at the
-// buffer's ends); its copy is cut where chunks meet.
+// preceding the call (2 x 1.8 GB took 6.1 ms up front).  The chunks and the
+// cut of each group's copy are ChunkPlan's.
 class ChunkLock {
 public:
-    ChunkLock(const void* p, size_t total, size_t step, bool enable)
-        : base_(static_cast<const char*>(p)), total_(total), step_(step), span_(p, total, page_size()) {
+    ChunkLock(const void* p, size_t total, size_t step, bool enable) {
         if (!p || !total) return;
         pinned_ = is_pinned(p);
         if (pinned_ || !enable) return;
-        chunks_ = (total + step - 1) / step;
-        regs_.assign(chunks_, false);
+        plan_ = ChunkPlan(uintptr_t(p), total, step, page_size());
+        regs_.assign(plan_.chunks, false);
         active_ = true;
     }
     ~ChunkLock() {
-        for (size_t k = 0; k < chunks_; ++k)
-            if (regs_[k]) cudaHostUnregister(reinterpret_cast<void*>(bound(k)));
+        for (size_t k = 0; k < regs_.size(); ++k)
+            if (regs_[k]) cudaHostUnregister(reinterpret_cast<void*>(plan_.bound(k)));
     }
     ChunkLock(const ChunkLock&) = delete;
     ChunkLock& operator=(const ChunkLock&) = delete;
     // Locks every chunk up to k (stops for good at the first refusal).
     void lock_through(size_t k) {
         if (!active_) return;
-        for (; ok_ && next_ <= k && next_ < chunks_; ++next_) {
-            const uintptr_t lo = bound(next_), hi = bound(next_ + 1);
+        for (; ok_ && next_ <= k && next_ < plan_.chunks; ++next_) {
+            const uintptr_t lo = plan_.bound(next_), hi = plan_.bound(next_ + 1);
             if (hi <= lo) continue;
             if (register_pages(lo, hi)) regs_[next_] = true;
             else ok_ = false;
@@ -480,51 +464,37 @@ public:
     }
     // The buffer is pinned or being locked: its copies go through copy_to_device.
     bool engaged() const { return pinned_ || active_; }
-    // Group k's bytes may be copied asynchronously.
-    bool usable(size_t k) const { return pinned_ || (active_ && ok_ && next_ > k); }
-    // Copies group k: its pieces in locked chunks asynchronously, its pieces in
-    // the buffer's partial end pages through `bounce` (pinned, two pages: head,
-    // tail), and pieces in chunks that could not be locked as pageable copies
-    // (the call returns once they are read).
-    void copy_to_device(char* dst, size_t k, size_t bytes, cudaStream_t st, char* bounce) const {
-        const char* src = base_ + k * step_;
+    // Copies group k (bytes from src): its pieces in locked chunks
+    // asynchronously, its pieces in the buffer's partial end pages through
+    // `bounce` (pinned, two pages: head, tail), and pieces in chunks that
+    // could not be locked as pageable copies (the call returns once they are
+    // read).  The bounce pages mirror the buffer's partial pages byte for
+    // byte, so groups that share one of them use disjoint bytes of it.
+    void copy_to_device(char* dst, const char* src, size_t k, size_t bytes, cudaStream_t st, char* bounce) {
         if (pinned_) {
             check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "input copy");
             return;
         }
-        const uintptr_t b = uintptr_t(src), e = b + bytes;
-        auto put = [&](uintptr_t x, uintptr_t y, const char* from) {
-            if (y > x) check(cudaMemcpyAsync(dst + (x - b), from, size_t(y - x), cudaMemcpyHostToDevice, st),
-                             "input copy");
-        };
-        // The bounce pages mirror the buffer's partial head and tail pages byte
-        // for byte, so groups that share one of them use disjoint bytes of it.
-        auto bounced = [&](uintptr_t x, uintptr_t y, char* mirror, uintptr_t origin) {
-            if (y <= x) return;
-            char* h = mirror + (x - origin);
-            std::memcpy(h, reinterpret_cast<const void*>(x), size_t(y - x));
-            put(x, y, h);
-        };
-        bounced(b, std::min(e, span_.lo), bounce, uintptr_t(base_));             // head page of the buffer
-        for (size_t j = 0; j < chunks_; ++j) {                      // whole pages, cut at chunk bounds
-            const uintptr_t x = std::max(b, uintptr_t(bound(j))), y = std::min(e, uintptr_t(bound(j + 1)));
-            put(x, y, reinterpret_cast<const char*>(x));
+        const uintptr_t b = uintptr_t(src);
+        group_pieces(plan_, k, pieces_);
+        for (const CopyPiece& c : pieces_) {
+            const char* from = reinterpret_cast<const char*>(c.lo);
+            if (c.kind != PieceKind::chunk) {
+                char* h = c.kind == PieceKind::head ? bounce + (c.lo - plan_.base)
+                                                    : bounce + page_size() + (c.lo - plan_.span.hi);
+                std::memcpy(h, from, size_t(c.hi - c.lo));
+                from = h;
+            }
+            check(cudaMemcpyAsync(dst + (c.lo - b), from, size_t(c.hi - c.lo), cudaMemcpyHostToDevice, st),
+                  "input copy");
         }
-        bounced(std::max(b, span_.hi), e, bounce + page_size(), span_.hi);       // tail page of the buffer
     }
 private:
-    uintptr_t bound(size_t k) const {
-        if (k == 0) return span_.lo;
-        if (k >= chunks_) return span_.hi;
-        const uintptr_t x = (uintptr_t(base_ + k * step_) + page_size() - 1) & ~(page_size() - 1);
-        return std::min(std::max(x, span_.lo), span_.hi);
-    }
-    const char* base_;
-    size_t total_, step_;
-    HostSpan span_;
-    size_t chunks_ = 0, next_ = 0;
+    ChunkPlan plan_;
+    size_t next_ = 0;
     bool pinned_ = false, active_ = false, ok_ = true;
     std::vector<bool> regs_;
+    std::vector<CopyPiece> pieces_;
 };
 
 // Page-locks the output runs of one call as they are named (a caller's
@@ -551,7 +521,7 @@ public:
             *hi = bytes;
             return;
         }
-        const HostSpan sp(d, bytes, page_size());
+        const PageSpan sp = whole_pages(b, bytes, page_size());
         if (sp.hi > sp.lo && register_pages(sp.lo, sp.hi)) {
             regs_.push_back(sp.lo);
             spans_.push_back({sp.lo, sp.hi});
@@ -651,6 +621,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     ensure_workspace(g);
     const uint32_t ngroups = (count + g - 1) / g;
     const uint32_t slots = std::min(kHostSlots, ngroups);
+
     constexpr size_t kPiece = size_t(4) << 20;
     ensure_host_slots(g, slots, !pageable_direct_ && !(is_pinned(a) && is_pinned(b)), !out_pinned);
     if (edge_.bytes < 4 * page_size()) edge_.allocate(4 * page_size());
@@ -666,7 +637,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     auto group_size = [&](uint32_t gi) { return std::min(g, count - gi * g); };
     auto stage_in = [&](ChunkLock& lk, uint32_t gi, char* h, char* d, const char* x, size_t bytes, char* bounce) {
         if (lk.engaged()) {                    // pinned or locked: asynchronous
-            lk.copy_to_device(d, gi, bytes, copy_in_, bounce);
+            lk.copy_to_device(d, x, gi, bytes, copy_in_, bounce);
             return;
         }
         if (pageable_direct_) {                // read in place (holds this thread for the transfer)
@@ -770,7 +741,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         uint32_t* d = io_dev_[s].as<uint32_t>();
         uint32_t* h = io_in_[s].ptr ? io_in_[s].as<uint32_t>() : nullptr;
         // Packing into the slot's staging: its previous inputs have left for the device.
-        const bool packs = !pageable_direct_ && !(lock_a.usable(gi) && lock_b_or_a.usable(gi));
+        const bool packs = !pageable_direct_ && !(lock_a.engaged() && lock_b_or_a.engaged());
         if (packs && gi >= slots) check(cudaEventSynchronize(ev_in_[s]), "slot reuse");
         if (gi >= slots) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
         // Operand A first: the device encodes it while operand B comes in.
@@ -817,7 +788,10 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
                                   cudaMemcpyDeviceToHost, copy_out_), "output copy");
         }
         check(cudaEventRecord(ev_out_[s], copy_out_), "event");
-        // Lock the next group's inputs while the device works on this one.
+        // Lock the next group's inputs while the device works on this one.  (On
+        // a helper thread running ahead, locking measured slower: 30.9 against
+        // 24.2 ms per B = 128 plugin call; the driver serialises it against
+        // this thread's calls.)
         lock_a.lock_through(gi + 1);
         lock_b_or_a.lock_through(gi + 1);
         if (!worker_out) continue;
