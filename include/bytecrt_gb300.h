@@ -139,8 +139,11 @@ int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_repo
 /* ---- whole products.
  * bcg_multiply: host buffers, synchronous; replaces fherma_run
  * (native-smoke/solve.cu:506-525; batched native-batched/solve.cu:200-244).
- * Pageable buffers are page-locked for the duration of the call (and
- * unlocked before it returns), so that every copy is asynchronous. */
+ * In calls of three or more groups of products, pageable buffers are
+ * page-locked as the call reaches them (the whole pages inside each buffer
+ * only; the partial pages at its ends go through pinned staging) and
+ * unlocked before it returns, so that the copies are asynchronous.  Pinned
+ * buffers are copied directly. */
 int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count);
 /* Like bcg_multiply, but the product ([count][N][L] words) is handed over in
  * order, in consecutive runs, to sink(user, words, n) as each run arrives on
