@@ -572,7 +572,7 @@ def run_native(args):
                 "link_frac": e2e_value / world / link_bound(link, 2 * N * L * 4, N * L * 4),
                 "link_model_even_split": link_model_even_split(link, 2 * N * L * 4, N * L * 4),
                 "step_ms": {"min": min(e2e_steps), "median": sorted(e2e_steps)[len(e2e_steps) // 2],
-                            "max": max(e2e_steps)},
+                            "max": max(e2e_steps), "each": [round(t, 2) for t in e2e_steps]},
                 "host_link": link},
         "stream_launch": {"products_per_s": stream_value, "ms_per_step": stream_ms / max(3, args.steps // 2)},
         "plain": {"device_ms_per_product": plain_ms, "device_products_per_s": 1000.0 / plain_ms,

@@ -23,7 +23,7 @@ SHIM = os.path.join(HERE, "libfherma_gb300.so")
 HARNESS = os.path.join(HERE, "solution")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CORE_SOURCES = ["plan.cu", "encode.cu", "encode_scalar.cu", "ntt.cu", "crt.cu", "crt_persistent.cu", "engine.cu", "capi.cu", "static_scratch.cu", "autotune.cu",
+CORE_SOURCES = ["plan.cu", "encode.cu", "encode_scalar.cu", "host_copy.cu", "ntt.cu", "crt.cu", "crt_persistent.cu", "engine.cu", "capi.cu", "static_scratch.cu", "autotune.cu",
                 "batch.cu", "server.cu", "capi_serve.cu"]
 
 

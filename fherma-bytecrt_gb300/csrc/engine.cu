@@ -588,15 +588,18 @@ private:
 
 // Host buffers.  Products move in groups of host_group() through kHostSlots
 // device slots ([A | B | C] each), so that one group's copies overlap the
-// compute of the others.  Inputs that are pinned (or locked for the call) go
-// in with asynchronous copies; otherwise they are read in place through the
-// host page tables where the GPU can (coherent CPU-GPU systems) or packed
-// into pinned staging.  A pinned output receives its products directly;
-// otherwise each group comes back into pinned staging with one copy, and the
-// output worker hands it, in order, to the sink (or copies it into c) while
-// the calling thread already issues the next groups.  A destination callback
-// names each group's output memory as the group is issued; the group is copied
-// straight into it where it can be page-locked, and through staging otherwise.
+// compute of the others.
+//  - Inputs: pinned ones go in with asynchronous copy-engine copies.  In calls
+//    of three or more groups, pageable ones are page-locked chunk by chunk
+//    just ahead of their copies.  In smaller calls the SMs read them in place
+//    where the GPU uses the host's page tables (coherent CPU-GPU systems, such
+//    as the GB300's Grace hosts); elsewhere they are packed into pinned staging.
+//  - Outputs: a pinned output receives its products directly.  A pageable
+//    output, or destinations a callback names group by group, is page-locked
+//    run by run in larger calls and written straight, and written by the SMs
+//    in smaller calls where the GPU uses the host's page tables.  A sink gets
+//    each group from pinned staging, in order: in larger calls on the output
+//    worker while the calling thread issues the next groups.
 void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count, Sink sink,
                             void* user, Dest dest) {
     if (count == 0) return;
@@ -640,8 +643,9 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
             lk.copy_to_device(d, x, gi, bytes, copy_in_, bounce);
             return;
         }
-        if (pageable_direct_) {                // read in place (holds this thread for the transfer)
-            check(cudaMemcpyAsync(d, x, bytes, cudaMemcpyHostToDevice, copy_in_), "input copy");
+        if (pageable_direct_) {                // the SMs read it in place, asynchronously
+            check(launch_host_copy(reinterpret_cast<uint32_t*>(d), reinterpret_cast<const uint32_t*>(x), bytes / 4,
+                                   copy_in_), "input copy");
             return;
         }
         for (size_t off = 0; off < bytes; off += kPiece) {
@@ -661,6 +665,11 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     // come back in 4 MiB pieces that this thread hands over as each lands (one
     // product through the plugin: 0.71 ms through the worker, 0.5 ms so).
     const bool inline_out = !out_pinned && ngroups <= 2;
+    // Small calls into memory the GPU can write through the host's page
+    // tables (a caller's destination or a pageable output): the SMs write
+    // the product there directly, right after the chain; the destination is
+    // named while the device computes.
+    const bool direct_out = inline_out && !sink && pageable_direct_;
     // Larger calls into a pageable output or a caller's destinations lock each
     // group's run of the output as it is issued and copy straight into it.
     const bool run_out = !out_pinned && !inline_out && !sink;
@@ -758,7 +767,11 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         });
         check(cudaEventRecord(ev_done_[s], stream_), "event");
         check(cudaStreamWaitEvent(copy_out_, ev_done_[s], 0), "event wait");
-        if (inline_out) {
+        if (direct_out) {
+            char* dst = named(gi, bytes / 4);
+            check(launch_host_copy(reinterpret_cast<uint32_t*>(dst), d + 2 * g * cw, bytes / 4, copy_out_),
+                  "output copy");
+        } else if (inline_out) {
             char* hs = reinterpret_cast<char*>(io_out_[s].as<uint32_t>());
             const char* ds = reinterpret_cast<const char*>(d + 2 * g * cw);
             for (size_t k = 0, po = 0; po < bytes; ++k, po += kPiece) {
@@ -800,7 +813,9 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         issued = gi + 1;
         cv.notify_all();
     }
-    if (inline_out) {
+    if (direct_out) {
+        check(cudaStreamSynchronize(copy_out_), "output copy");
+    } else if (inline_out) {
         for (uint32_t gi = 0; gi < ngroups; ++gi) {
             const uint32_t s = gi % slots;
             const size_t bytes = size_t(group_size(gi)) * cw * 4;

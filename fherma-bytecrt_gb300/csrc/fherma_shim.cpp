@@ -17,24 +17,17 @@
 #include <memory>
 #include <mutex>
 #include <omp.h>
-#include <sys/mman.h>
-#include <unistd.h>
-
-#ifndef MADV_POPULATE_WRITE
-#define MADV_POPULATE_WRITE 23   // Linux 5.14
-#endif
-
-// The owned output vector is built in one of two ways.  Small outputs are
-// appended run by run as each staged run arrives (no zero fill first).  Large
-// ones grow run by run as the library names each group's destination: the
-// vector's resize zero-fills the run, and the library copies the group
-// straight into it (page-locked), so the host writes each output byte once
-// besides the copy engine and no staging copy follows the device work
-// (B = 128 at N = 65536: 29.7 ms per call with one zero fill up front,
-// against 38.2 ms through staging).  std::vector copies with memmove/memcpy
-// and fills with memset; this library is linked with --wrap for all three, so
-// that large copies and fills (and the first touch of fresh pages) run on all
-// cores, as the reference does for its output (native-smoke/vector-copy.cpp:19-56).
+// The owned output vector grows run by run as the library names each group's
+// destination (bcg_multiply_dest): the vector's resize zero-fills the run, and
+// the library writes the group straight into it (copy engine into page-locked
+// runs in larger calls, SM stores through the host page tables in small ones),
+// so the host writes each output byte once and no staging copy follows the
+// device work.  B = 128 at N = 65536 took 38.2 ms per call when each group was
+// staged and appended instead, 24-28 ms so.  std::vector copies with
+// memmove/memcpy and fills with memset; this library is linked with --wrap for
+// all three, so that large copies and fills (and the first touch of fresh
+// pages) run on all cores, as the reference does for its output
+// (native-smoke/vector-copy.cpp:19-56).
 extern "C" void* __real_memcpy(void* dst, const void* src, size_t n);
 extern "C" void* __real_memmove(void* dst, const void* src, size_t n);
 extern "C" void* __real_memset(void* dst, int c, size_t n);
@@ -42,9 +35,6 @@ extern "C" void* __real_memset(void* dst, int c, size_t n);
 namespace {
 
 constexpr size_t kParallelBytes = size_t(1) << 20;
-// Outputs from this size up take the destination path (a few host groups at
-// N = 65536; below it the staged append is as fast and fills nothing).
-constexpr size_t kDestBytes = size_t(128) << 20;
 
 void parallel_copy(char* dst, const char* src, size_t n) {
     const int workers = omp_get_num_procs() < 16 ? omp_get_num_procs() : 16;
@@ -63,27 +53,6 @@ void parallel_fill(char* dst, int c, size_t n) {
     for (int t = 0; t < workers; ++t) {
         const size_t begin = size_t(t) * chunk;
         if (begin < n) __real_memset(dst + begin, c, n - begin < chunk ? n - begin : chunk);
-    }
-}
-
-// Faults in the pages of [p, p + n) on all cores (the kernel zero-fills them),
-// so that appending the product later only copies.  Best effort: an older
-// kernel without MADV_POPULATE_WRITE leaves the faults to the copies.
-void populate(void* p, size_t n) {
-    const uintptr_t page = uintptr_t(sysconf(_SC_PAGESIZE));
-    const uintptr_t begin = (uintptr_t(p) + page - 1) & ~(page - 1);
-    const uintptr_t end = (uintptr_t(p) + n) & ~(page - 1);
-    if (end <= begin) return;
-    const size_t pages = (end - begin) / page;
-    const int workers = omp_get_num_procs() < 16 ? omp_get_num_procs() : 16;
-    const size_t per = (pages + workers - 1) / workers;
-#pragma omp parallel for num_threads(workers) schedule(static)
-    for (int t = 0; t < workers; ++t) {
-        const size_t first = size_t(t) * per;
-        if (first < pages) {
-            const size_t count = pages - first < per ? pages - first : per;
-            madvise(reinterpret_cast<void*>(begin + first * page), count * page, MADV_POPULATE_WRITE);
-        }
     }
 }
 
@@ -178,53 +147,30 @@ fherma::Outputs fherma_run(void* state, const fherma::Inputs& in) {
     out.c.shape = {int64_t(s.N), int64_t(s.L)};
 #endif
     out.c.data.reserve(total);
-    if (total * sizeof(uint32_t) >= kDestBytes) {
-        // Large outputs: each group lands straight in the vector, grown (and
-        // zero-filled) run by run on the calling thread as the library names it.
-        struct Grow {
-            std::vector<uint32_t>* v;
-            std::exception_ptr error;
-        } grow{&out.c.data, nullptr};
-        const int rc = bcg_multiply_dest(s.ctx, in.a.data.data(), in.b.data.data(), s.B,
-                                         [](void* user, size_t n) -> uint32_t* {
-                                             auto* g = static_cast<Grow*>(user);
-                                             const size_t at = g->v->size();
-                                             // Never past the reserved capacity: earlier runs keep their addresses.
-                                             if (at + n > g->v->capacity()) return nullptr;
-                                             try {
-                                                 g->v->resize(at + n);
-                                             } catch (...) {
-                                                 g->error = std::current_exception();
-                                                 return nullptr;
-                                             }
-                                             return g->v->data() + at;
-                                         },
-                                         &grow);
-        if (grow.error) std::rethrow_exception(grow.error);
-        check(rc, "run");
-    } else {
-        struct Append {
-            std::vector<uint32_t>* v;
-            std::exception_ptr error;
-        } sink{&out.c.data, nullptr};
-        check(bcg_multiply_sink(s.ctx, in.a.data.data(), in.b.data.data(), s.B,
-                                [](void* user, const uint32_t* words, size_t n) {
-                                    auto* app = static_cast<Append*>(user);
-                                    if (app->error) return;
-                                    if (!words) {   // the device is busy: fault in the output pages
-                                        populate(app->v->data() + app->v->size(), n * sizeof(uint32_t));
-                                        return;
-                                    }
-                                    try {
-                                        app->v->insert(app->v->end(), words, words + n);
-                                    } catch (...) {
-                                        app->error = std::current_exception();
-                                    }
-                                },
-                                &sink),
-              "run");
-        if (sink.error) std::rethrow_exception(sink.error);
-    }
+    // The vector grows run by run (zero-filled on up to 16 threads) as the
+    // library names each group's destination, and the library writes the
+    // products straight into it.
+    struct Grow {
+        std::vector<uint32_t>* v;
+        std::exception_ptr error;
+    } grow{&out.c.data, nullptr};
+    const int rc = bcg_multiply_dest(s.ctx, in.a.data.data(), in.b.data.data(), s.B,
+                                     [](void* user, size_t n) -> uint32_t* {
+                                         auto* g = static_cast<Grow*>(user);
+                                         const size_t at = g->v->size();
+                                         // Never past the reserved capacity: earlier runs keep their addresses.
+                                         if (at + n > g->v->capacity()) return nullptr;
+                                         try {
+                                             g->v->resize(at + n);
+                                         } catch (...) {
+                                             g->error = std::current_exception();
+                                             return nullptr;
+                                         }
+                                         return g->v->data() + at;
+                                     },
+                                     &grow);
+    if (grow.error) std::rethrow_exception(grow.error);
+    check(rc, "run");
     if (out.c.data.size() != total) throw std::runtime_error("bytecrt-gb300 output size");
     return out;
 }

@@ -91,4 +91,8 @@ cudaError_t launch_row_product(const NttArgs& a, const uint32_t* planes_a, size_
 cudaError_t launch_row_forward(const NttArgs& a, uint32_t* planes, size_t stride, uint32_t nplanes, cudaStream_t st);
 size_t row_smem_bytes(const NttArgs& a, bool forward_only);
 
+// Word copy with SM loads and stores (host_copy.cu); either side may be
+// pageable host memory where the GPU uses the host's page tables.
+cudaError_t launch_host_copy(uint32_t* dst, const uint32_t* src, size_t words, cudaStream_t st);
+
 }  // namespace bcg

@@ -164,9 +164,11 @@ int bcg_multiply_sink(bcg_context* ctx, const uint32_t* a, const uint32_t* b, ui
  * count n and returns where those n words go (host memory that the caller
  * neither reads nor writes until the call returns; NULL fails the call with
  * BCG_ERR_INVALID).  Every run is named before any of its words is written.
- * The library page-locks each run as it is named (runs that follow one
- * another in one buffer share their boundary pages) and copies the product
- * straight into it; what cannot be locked comes back through pinned staging.
+ * In calls of three or more groups the library page-locks the whole pages of
+ * each run as it is named and copies the product straight into them (the
+ * partial pages at a run's ends, and runs that cannot be locked, come back
+ * through pinned staging).  In smaller calls, where the GPU uses the host's
+ * page tables, the SMs write the product straight into the run.
  * For callers that grow their own output run by run while earlier groups
  * compute (the plugin's owned std::vector: its zero fill overlaps the device
  * work instead of a staging copy after it).  No counterpart in the reference. */
