@@ -73,6 +73,11 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # nvidia-smi's start-up (NVML initialisation) stalls the GPU's work for
+            # some 20 ms: the timed region starts once it samples.
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.005)
         except OSError:
             self.proc = None
         return self
@@ -482,13 +487,14 @@ def run_native(args):
         m.multiply_into(a_h, b_h, c_h, B)
     link_before = host_link(a_h, a_dev, c_h, c_dev)
     barrier()
-    t0 = time.perf_counter()
-    e2e_steps = []
-    for _ in range(args.steps):
-        ts = time.perf_counter()
-        m.multiply_into(a_h, b_h, c_h, B)
-        e2e_steps.append(1000.0 * (time.perf_counter() - ts))
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    with ClockSampler(local) as e2e_clocks:
+        t0 = time.perf_counter()
+        e2e_steps = []
+        for _ in range(args.steps):
+            ts = time.perf_counter()
+            m.multiply_into(a_h, b_h, c_h, B)
+            e2e_steps.append(1000.0 * (time.perf_counter() - ts))
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
     barrier()
     e2e_value = world * B * args.steps / e2e_s
     assert torch.equal(c_h[0], c0), "host path and device path disagree"
@@ -573,6 +579,7 @@ def run_native(args):
                 "link_model_even_split": link_model_even_split(link, 2 * N * L * 4, N * L * 4),
                 "step_ms": {"min": min(e2e_steps), "median": sorted(e2e_steps)[len(e2e_steps) // 2],
                             "max": max(e2e_steps), "each": [round(t, 2) for t in e2e_steps]},
+                "clocks": e2e_clocks.summary(),
                 "host_link": link},
         "stream_launch": {"products_per_s": stream_value, "ms_per_step": stream_ms / max(3, args.steps // 2)},
         "plain": {"device_ms_per_product": plain_ms, "device_products_per_s": 1000.0 / plain_ms,
@@ -999,7 +1006,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
-    ap.add_argument("--cpu-sample", type=int, default=4, help="products in the CPU baseline sample (0: skip)")
+    ap.add_argument("--cpu-sample", type=int, default=24,
+                    help="products in the CPU baseline sample, about 10 s on 16 Arm cores (0: skip)")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu case and exit")
     ap.add_argument("--profile-count", type=int, default=2)
     ap.add_argument("--group", type=int, default=0, help="products per launch chain (0: library default)")

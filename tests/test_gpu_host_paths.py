@@ -136,13 +136,16 @@ def test_dest_runs_fill_one_buffer(N, W, count):
     m.close()
 
 
+@pytest.mark.parametrize("count", [1, 10])
 @pytest.mark.parametrize("layout", ["separate", "reversed", "pinned"])
-def test_dest_layouts(layout):
-    """Runs in separate buffers, runs placed back to front in one buffer (each
-    run's last page is locked already: its tail comes back through staging),
-    and runs in pinned memory: the same products as the device path."""
+def test_dest_layouts(layout, count):
+    """Runs in separate buffers, runs placed back to front in one buffer, and
+    runs in pinned memory, in a small call (one group: written by the SMs where
+    the GPU uses the host page tables) and a larger one (three groups: whole
+    pages locked run by run, partial pages through staging): the same products
+    as the device path."""
     pkg = package()
-    N, W, count = 65536, 1747, 10
+    N, W = 65536, 1747
     q = pkg.inputs.modulus(W, 36)
     m = pkg.Multiplier(N, W, q)
     a, b = operands(pkg, q, N, count, 600)
