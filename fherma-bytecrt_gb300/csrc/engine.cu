@@ -606,8 +606,8 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     const size_t cw = coeff_words();
     const size_t all = size_t(count) * cw * 4;
     // Locking pays where the groups overlap one another's copies; a call of one
-    // or two groups (one product: 0.50 against 0.81 ms through the plugin) keeps
-    // the pageable path.
+    // or two groups is not locked (one product through the plugin: 0.50 ms
+    // unlocked against 0.81 ms locked, 0.42 ms with the copy kernels below).
     const uint32_t g = std::min(host_group(), count);
     const size_t gbytes = size_t(g) * cw * 4;
     const bool lock = count > 2 * g;
