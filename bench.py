@@ -477,7 +477,10 @@ def run_native(args):
     torch.cuda.synchronize()
     plain_ms = s2.elapsed_time(e2) / plain_iters
 
-    # ---- end to end through the host API from pinned memory.
+    # ---- end to end through the host API from pinned memory.  The timed window runs in a worker process
+    # that does not load torch (run_e2e_worker): calls from a process that has initialised torch stall now
+    # and then (every ~0.5 s, 7-150 ms), and the same calls from a torch-free process do not.  This process
+    # keeps its own window beside it as `in_process_torch`.
     a_h = torch.empty((B, N, L), dtype=torch.int32).pin_memory()
     b_h = torch.empty((B, N, L), dtype=torch.int32).pin_memory()
     c_h = torch.empty((B, N, L), dtype=torch.int32).pin_memory()
@@ -486,28 +489,55 @@ def run_native(args):
     for _ in range(max(1, args.warmup)):
         m.multiply_into(a_h, b_h, c_h, B)
     link_before = host_link(a_h, a_dev, c_h, c_dev)
+    knobs = {k: m.get_tuning(k) for k in ("group", "crt_tiles", "crt_persistent", "row_local", "row_rows",
+                                           "row_bits", "row_pass", "encode_scalar")}
+    barrier()
+    worker = subprocess.run([sys.executable, os.path.abspath(__file__), "--e2e-worker", "--e2e-device", str(local),
+                             "--e2e-seed", str(1000 + 97 * rank), "--e2e-tuning", json.dumps(knobs),
+                             "--steps", str(args.steps), "--warmup", str(args.warmup)],
+                            capture_output=True, text=True, timeout=600)
+    try:
+        w = json.loads(worker.stdout.strip().splitlines()[-1])
+    except (IndexError, ValueError):
+        w = {"error": (worker.stderr or worker.stdout)[-300:]}
     barrier()
     with ClockSampler(local) as e2e_clocks:
         t0 = time.perf_counter()
-        e2e_steps = []
+        in_steps = []
         for _ in range(args.steps):
             ts = time.perf_counter()
             m.multiply_into(a_h, b_h, c_h, B)
-            e2e_steps.append(1000.0 * (time.perf_counter() - ts))
-        e2e_s = max_over_ranks(time.perf_counter() - t0)
-    barrier()
-    e2e_value = world * B * args.steps / e2e_s
+            in_steps.append(1000.0 * (time.perf_counter() - ts))
+        in_s = time.perf_counter() - t0
     assert torch.equal(c_h[0], c0), "host path and device path disagree"
     for _ in range(2):
         m.multiply_into(a_h[0], b_h[0], c_h[0], 1)
     t0 = time.perf_counter()
     for i in range(plain_iters):
         m.multiply_into(a_h[i % DISTINCT], b_h[i % DISTINCT], c_h[i % DISTINCT], 1)
-    plain_e2e_ms = 1000 * (time.perf_counter() - t0) / plain_iters
+    in_plain_ms = 1000 * (time.perf_counter() - t0) / plain_iters
     # The link is shared with the rest of the host: its rate moves between runs, so the bound takes the
     # better of a measurement just before and one just after the e2e window.
     link = best_link(link_before, host_link(a_h, a_dev, c_h, c_dev))
     del a_h, b_h, c_h
+    import hashlib
+    want_hashes = [hashlib.sha256(c_dev[i].cpu().numpy().tobytes()).hexdigest() for i in range(DISTINCT)]
+    in_process = {"value": B * args.steps / in_s, "plain_ms_per_product": in_plain_ms,
+                  "step_ms": {"min": min(in_steps), "median": sorted(in_steps)[len(in_steps) // 2],
+                              "max": max(in_steps), "each": [round(t, 2) for t in in_steps]},
+                  "clocks": e2e_clocks.summary()}
+    if "seconds" in w:
+        if w.get("hashes") != want_hashes:
+            raise AssertionError("the e2e worker's products differ from the device path's")
+        e2e_s = max_over_ranks(w["seconds"])
+        e2e_steps, plain_e2e_ms, e2e_clock = w["step_ms"], w["plain_ms_per_product"], w.get("clocks")
+        e2e_where = ("a worker process without torch (pinned buffers from bcg_host_alloc); every distinct "
+                     "product's sha256 equals the device path's")
+    else:
+        e2e_s = max_over_ranks(in_s)
+        e2e_steps, plain_e2e_ms, e2e_clock = in_steps, in_plain_ms, in_process["clocks"]
+        e2e_where = "this process (the torch-free worker failed: " + str(w.get("error"))[:200] + ")"
+    e2e_value = world * B * args.steps / e2e_s
 
     uneven = run_uneven(pkg, args, stream, local) if args.uneven else None
     encode_kernels = run_encode_kernels(pkg, stream, local) if args.encode_kernels and rank == 0 else None
@@ -579,7 +609,7 @@ def run_native(args):
                 "link_model_even_split": link_model_even_split(link, 2 * N * L * 4, N * L * 4),
                 "step_ms": {"min": min(e2e_steps), "median": sorted(e2e_steps)[len(e2e_steps) // 2],
                             "max": max(e2e_steps), "each": [round(t, 2) for t in e2e_steps]},
-                "clocks": e2e_clocks.summary(),
+                "clocks": e2e_clock, "measured_in": e2e_where, "in_process_torch": in_process,
                 "host_link": link},
         "stream_launch": {"products_per_s": stream_value, "ms_per_step": stream_ms / max(3, args.steps // 2)},
         "plain": {"device_ms_per_product": plain_ms, "device_products_per_s": 1000.0 / plain_ms,
@@ -600,6 +630,56 @@ def run_native(args):
     batch.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_e2e_worker(args):
+    """The e2e window of run_native, in a process that does not load torch:
+    B=128 products per bcg_multiply call from pinned host buffers
+    (bcg_host_alloc), W warm-up calls, K timed calls, then one product per
+    call; prints one JSON line with each call's time and the sha256 of each
+    distinct product."""
+    import ctypes
+    import hashlib
+    import numpy as np
+    pkg = importlib.import_module("fherma-bytecrt_gb300")
+    q, a_np, b_np = make_inputs(pkg, args.e2e_seed)
+    L = (W + 31) // 32
+    m = pkg.Multiplier(N, W, q, device=args.e2e_device)
+    for k, v in json.loads(args.e2e_tuning or "{}").items():
+        m.set_tuning(k, v)
+    words = N * L
+    nbytes = B * words * 4
+    pa, pb, pc = (pkg.native.host_alloc(nbytes, args.e2e_device) for _ in range(3))
+    try:
+        idx = np.arange(B) % DISTINCT
+        for ptr, x in ((pa, a_np), (pb, b_np)):
+            src = np.ascontiguousarray(x[idx])
+            ctypes.memmove(ptr, src.ctypes.data, nbytes)
+        for _ in range(max(1, args.warmup)):
+            m.multiply_into(pa, pb, pc, B)
+        steps = []
+        with ClockSampler(args.e2e_device) as clocks:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                ts = time.perf_counter()
+                m.multiply_into(pa, pb, pc, B)
+                steps.append(1000.0 * (time.perf_counter() - ts))
+            seconds = time.perf_counter() - t0
+        out = np.ctypeslib.as_array((ctypes.c_uint32 * (B * words)).from_address(pc))
+        hashes = [hashlib.sha256(out[i * words:(i + 1) * words].tobytes()).hexdigest() for i in range(DISTINCT)]
+        plain_iters = max(3, args.steps)
+        for _ in range(2):
+            m.multiply_into(pa, pb, pc, 1)
+        t0 = time.perf_counter()
+        for i in range(plain_iters):
+            off = (i % DISTINCT) * words * 4
+            m.multiply_into(pa + off, pb + off, pc + off, 1)
+        plain_ms = 1000 * (time.perf_counter() - t0) / plain_iters
+    finally:
+        for ptr in (pa, pb, pc):
+            pkg.native.host_free(ptr)
+    print(json.dumps({"seconds": seconds, "step_ms": steps, "plain_ms_per_product": plain_ms, "hashes": hashes,
+                      "clocks": clocks.summary()}), flush=True)
 
 
 def run_encode_kernels(pkg, stream, device=0):
@@ -1035,8 +1115,14 @@ def main():
                     help="p99 latency target: the served figure is the highest sustained rate that meets it")
     ap.add_argument("--served-bisect", type=int, default=3,
                     help="offered-load bisection steps toward the p99 target")
+    ap.add_argument("--e2e-worker", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--e2e-device", type=int, default=0, help=argparse.SUPPRESS)
+    ap.add_argument("--e2e-seed", type=int, default=1000, help=argparse.SUPPRESS)
+    ap.add_argument("--e2e-tuning", default="", help=argparse.SUPPRESS)
     args = ap.parse_args()
-    if args.profile_case:
+    if args.e2e_worker:
+        run_e2e_worker(args)
+    elif args.profile_case:
         run_profile_case(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -202,6 +202,22 @@ int bcg_multiply_dest(bcg_context* ctx, const uint32_t* a, const uint32_t* b, ui
     });
 }
 
+int bcg_host_alloc(size_t bytes, int device, void** out) {
+    return guarded([&] {
+        require(out, "null argument");
+        *out = nullptr;
+        require(bytes > 0, "zero-byte allocation");
+        bcg::check(cudaSetDevice(device), "select device");
+        bcg::check(cudaMallocHost(out, bytes), "pinned allocation");
+    });
+}
+
+int bcg_host_free(void* p) {
+    return guarded([&] {
+        if (p) bcg::check(cudaFreeHost(p), "pinned free");
+    });
+}
+
 int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t* c, uint32_t count) {
     return guarded([&] {
         require(ctx, "null context");

@@ -102,6 +102,8 @@ def lib():
         L.bcg_context_set_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
         L.bcg_context_get_tuning.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]
         L.bcg_multiply.argtypes = [vp, _u32p, _u32p, _u32p, ctypes.c_uint32]
+        L.bcg_host_alloc.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(vp)]
+        L.bcg_host_free.argtypes = [vp]
         L.bcg_multiply_sink.argtypes = [vp, _u32p, _u32p, ctypes.c_uint32, SINK, vp]
         L.bcg_multiply_dest.argtypes = [vp, _u32p, _u32p, ctypes.c_uint32, DEST, vp]
         L.bcg_context_autotune.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(bcg_autotune_report)]
@@ -189,6 +191,17 @@ class Plan:
         w = np.zeros((self.P + 1) * self.L, np.uint32)
         _check(lib().bcg_plan_weights(self._h, _p(w)))
         return w.reshape(self.P + 1, self.L)
+
+
+def host_alloc(nbytes: int, device: int = 0) -> int:
+    """Pinned host memory (bcg_host_alloc): the address of nbytes; free with host_free."""
+    p = ctypes.c_void_p()
+    _check(lib().bcg_host_alloc(nbytes, device, ctypes.byref(p)))
+    return p.value
+
+
+def host_free(address: int) -> None:
+    _check(lib().bcg_host_free(address))
 
 
 class Multiplier:

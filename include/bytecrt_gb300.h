@@ -136,6 +136,13 @@ typedef struct bcg_autotune_report {
 } bcg_autotune_report;
 int bcg_context_autotune(bcg_context* ctx, uint32_t max_group, bcg_autotune_report* out);
 
+/* ---- pinned host memory for the fastest host-buffer calls: bcg_multiply copies
+ * pinned operands and outputs with asynchronous copy-engine copies, overlapped
+ * with the device's work, and locks nothing.  The reference keeps pinned
+ * staging of its own (native-smoke/solve.cu:191-247).  Free with bcg_host_free. */
+int bcg_host_alloc(size_t bytes, int device, void** out);
+int bcg_host_free(void* p);
+
 /* ---- whole products.
  * bcg_multiply: host buffers, synchronous; replaces fherma_run
  * (native-smoke/solve.cu:506-525; batched native-batched/solve.cu:200-244).

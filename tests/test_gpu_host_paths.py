@@ -195,3 +195,25 @@ def test_dest_refusal_fails_the_call_and_keeps_the_context():
     assert len(named) == 2
     assert np.array_equal(m.multiply(a, b), device_products(m, a, b))
     m.close()
+
+
+def test_host_alloc_buffers():
+    """Pinned buffers from bcg_host_alloc take the direct copy path and give the device path's products."""
+    import ctypes
+    pkg = package()
+    N, W, count = 16384, 434, 80
+    q = pkg.inputs.modulus(W, 38)
+    m = pkg.Multiplier(N, W, q)
+    a, b = operands(pkg, q, N, count, 800)
+    nbytes = a.nbytes
+    pa, pb, pc = (pkg.native.host_alloc(nbytes) for _ in range(3))
+    try:
+        ctypes.memmove(pa, a.ctypes.data, nbytes)
+        ctypes.memmove(pb, b.ctypes.data, nbytes)
+        m.multiply_into(pa, pb, pc, count)
+        got = np.ctypeslib.as_array((ctypes.c_uint32 * a.size).from_address(pc)).reshape(a.shape).copy()
+    finally:
+        for p in (pa, pb, pc):
+            pkg.native.host_free(p)
+    assert np.array_equal(got, device_products(m, a, b))
+    m.close()
