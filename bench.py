@@ -541,7 +541,22 @@ def run_native(args):
 
     uneven = run_uneven(pkg, args, stream, local) if args.uneven else None
     encode_kernels = run_encode_kernels(pkg, stream, local) if args.encode_kernels and rank == 0 else None
-    served = run_served(pkg, args, local, value, e2e_value) if args.served else None
+    served = None
+    if args.served:
+        # Like the e2e window, the request loop runs in a worker that does not load torch.
+        cmd = [sys.executable, os.path.abspath(__file__), "--served-worker", "--e2e-device", str(local),
+               "--served-batched", repr(value / world), "--served-e2e", repr(e2e_value / world)]
+        for flag in ("served_loads", "served_seconds", "served_requests", "served_slots", "served_max_batch",
+                     "served_p99_ms", "served_bisect"):
+            cmd += ["--" + flag.replace("_", "-"), str(getattr(args, flag))]
+        if not args.autotune:
+            cmd.append("--no-autotune")
+        sw = subprocess.run(cmd, capture_output=True, text=True, timeout=1800)
+        try:
+            served = json.loads(sw.stdout.strip().splitlines()[-1])
+            served["measured_in"] = "a worker process without torch (pinned buffers from bcg_host_alloc)"
+        except (IndexError, ValueError):
+            served = {"error": (sw.stderr or sw.stdout)[-300:]}
 
     if rank != 0:
         if world > 1:
@@ -680,6 +695,13 @@ def run_e2e_worker(args):
             pkg.native.host_free(ptr)
     print(json.dumps({"seconds": seconds, "step_ms": steps, "plain_ms_per_product": plain_ms, "hashes": hashes,
                       "clocks": clocks.summary()}), flush=True)
+
+
+def run_served_worker(args):
+    """run_served in a process that does not load torch (see run_native); prints its result as one JSON line."""
+    pkg = importlib.import_module("fherma-bytecrt_gb300")
+    out = run_served(pkg, args, args.e2e_device, args.served_batched, args.served_e2e or None)
+    print(json.dumps(out), flush=True)
 
 
 def run_encode_kernels(pkg, stream, device=0):
@@ -893,9 +915,18 @@ def run_served(pkg, args, device, batched_value, e2e_value=None):
     alone.  Beside the sweep, the offered load is bisected for the highest
     sustained rate whose p99 meets --served-p99-ms."""
     from concurrent.futures import ThreadPoolExecutor
+    import ctypes
     import numpy as np
-    import torch
     autotune_geometries(pkg, args, device, [(16384, 434), (32768, 868), (65536, 1747)])
+    pinned = []
+
+    def pinned_array(shape):
+        """A uint32 numpy array over pinned host memory from bcg_host_alloc."""
+        count = int(np.prod(shape))
+        addr = pkg.native.host_alloc(count * 4, device)
+        pinned.append(addr)
+        return np.ctypeslib.as_array((ctypes.c_uint32 * count).from_address(addr)).reshape(shape)
+
     srv = pkg.Server(device, slots=args.served_slots, max_batch=args.served_max_batch)
     mix = [((16384, 434), 0.3, 1), ((32768, 868), 0.4, 2), ((65536, 1747), 0.3, 2)]
     points = []   # (n, w, q, pid, a pool, b pool, resident ids, out ring)
@@ -904,11 +935,11 @@ def run_served(pkg, args, device, batched_value, e2e_value=None):
             q = pkg.inputs.modulus(w, 9000 + 17 * k + w)
             pid = srv.add_point(n, w, q)
             l = (w + 31) // 32
-            pool = torch.empty((8, n, l), dtype=torch.int32).pin_memory()
+            pool = pinned_array((8, n, l))
             for i in range(8):
-                pool[i].copy_(torch.from_numpy(pkg.inputs.uniform(q, n, 100 * k + i).view(np.int32)))
+                pool[i] = pkg.inputs.uniform(q, n, 100 * k + i)
             res = [srv.add_operand(pid, pool[i]) for i in (0, 1)]
-            ring = torch.empty((48, n, l), dtype=torch.int32).pin_memory()
+            ring = pinned_array((48, n, l))
             points.append(dict(n=n, w=w, q=q, pid=pid, pool=pool, res=res, ring=ring, share=share / nq,
                                slot=0, owner=[None] * 48))
     shares = np.array([p["share"] for p in points])
@@ -932,8 +963,7 @@ def run_served(pkg, args, device, batched_value, e2e_value=None):
         mult = pkg.Multiplier(p["n"], p["w"], p["q"], device=device)
         for ai in range(4):
             for bi in range(4, 8):
-                alone[(pi, ai, bi)] = mult.multiply(p["pool"][ai].numpy().view(np.uint32),
-                                                   p["pool"][bi].numpy().view(np.uint32))
+                alone[(pi, ai, bi)] = mult.multiply(p["pool"][ai], p["pool"][bi])
         mult.close()
     compare = ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4))
 
@@ -962,7 +992,7 @@ def run_served(pkg, args, device, batched_value, e2e_value=None):
             pi, a_i, b_i, slot = pending.pop(rid)
             lat.append(srv.wait(rid))
             if verify:
-                got = points[pi]["ring"][slot].numpy().view(np.uint32)
+                got = points[pi]["ring"][slot]
                 checks[(pi, slot)] = compare.submit(np.array_equal, got, alone[(pi, a_i, b_i)])
 
         def settle(key):
@@ -1039,6 +1069,8 @@ def run_served(pkg, args, device, batched_value, e2e_value=None):
     stats = srv.stats()
     srv.close()
     compare.shutdown()
+    for addr in pinned:
+        pkg.native.host_free(addr)
     every = results + bisect
     saturated = max(every, key=lambda r: r["sustained_per_s"])
     at_target = max((r for r in every if r["p99_ms"] <= target), key=lambda r: r["sustained_per_s"], default=None)
@@ -1116,12 +1148,17 @@ def main():
     ap.add_argument("--served-bisect", type=int, default=3,
                     help="offered-load bisection steps toward the p99 target")
     ap.add_argument("--e2e-worker", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--served-worker", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--served-batched", type=float, default=0.0, help=argparse.SUPPRESS)
+    ap.add_argument("--served-e2e", type=float, default=0.0, help=argparse.SUPPRESS)
     ap.add_argument("--e2e-device", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--e2e-seed", type=int, default=1000, help=argparse.SUPPRESS)
     ap.add_argument("--e2e-tuning", default="", help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.e2e_worker:
         run_e2e_worker(args)
+    elif args.served_worker:
+        run_served_worker(args)
     elif args.profile_case:
         run_profile_case(args)
     elif args.impl == "reference":
