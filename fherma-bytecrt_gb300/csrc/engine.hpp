@@ -213,7 +213,8 @@ private:
     PinnedBuffer io_in_[kHostSlots], io_out_[kHostSlots];
     PinnedBuffer edge_;   // partial end pages of the operands (two pages per operand)
     cudaEvent_t ev_in_[kHostSlots] = {}, ev_done_[kHostSlots] = {}, ev_out_[kHostSlots] = {};
-    cudaEvent_t ev_host_[kHostSlots] = {};   // staged output landed (waited on by the output worker only)
+    cudaEvent_t ev_host_[kHostSlots] = {};   // staged output landed (host waits only: the output worker, and
+                                             // the calling thread for a run's staged end pages)
     std::vector<cudaEvent_t> piece_ev_[kHostSlots];   // 4 MiB output pieces of small calls
     std::unique_ptr<HostWorker> worker_;   // output side of the host path (created on first use)
     NttArgs ntt_{};
