@@ -30,9 +30,10 @@ def device_products(m, a, b):
     return dc.cpu().numpy().view(np.uint32)
 
 
-# (N, W, count): the last two take three host groups (the staging groups hold
-# about 128 MiB of operands: 4 products at N=65536, 71 at N=16384).
-CASES = [(4096, 868, 5), (65536, 1747, 9), (16384, 434, 150)]
+# (N, W, count): one host group, two (still a small call: no page locking), and
+# three or more (the staging groups hold about 128 MiB of operands: 4 products
+# at N=65536, 32 at N=16384).
+CASES = [(4096, 868, 5), (65536, 1747, 6), (65536, 1747, 9), (16384, 434, 150)]
 
 
 @pytest.mark.parametrize("N,W,count", CASES)
