@@ -492,12 +492,14 @@ def run_native(args):
     knobs = {k: m.get_tuning(k) for k in ("group", "crt_tiles", "crt_persistent", "row_local", "row_rows",
                                            "row_bits", "row_pass", "encode_scalar")}
     barrier()
-    worker = subprocess.run([sys.executable, os.path.abspath(__file__), "--e2e-worker", "--e2e-device", str(local),
-                             "--e2e-seed", str(1000 + 97 * rank), "--e2e-tuning", json.dumps(knobs),
-                             "--steps", str(args.steps), "--warmup", str(args.warmup)],
-                            capture_output=True, text=True, timeout=600)
     try:
+        worker = subprocess.run([sys.executable, os.path.abspath(__file__), "--e2e-worker", "--e2e-device",
+                                 str(local), "--e2e-seed", str(1000 + 97 * rank), "--e2e-tuning", json.dumps(knobs),
+                                 "--steps", str(args.steps), "--warmup", str(args.warmup)],
+                                capture_output=True, text=True, timeout=600)
         w = json.loads(worker.stdout.strip().splitlines()[-1])
+    except subprocess.TimeoutExpired:
+        w = {"error": "the worker ran past 600 s"}
     except (IndexError, ValueError):
         w = {"error": (worker.stderr or worker.stdout)[-300:]}
     barrier()
@@ -551,10 +553,12 @@ def run_native(args):
             cmd += ["--" + flag.replace("_", "-"), str(getattr(args, flag))]
         if not args.autotune:
             cmd.append("--no-autotune")
-        sw = subprocess.run(cmd, capture_output=True, text=True, timeout=1800)
         try:
+            sw = subprocess.run(cmd, capture_output=True, text=True, timeout=1800)
             served = json.loads(sw.stdout.strip().splitlines()[-1])
             served["measured_in"] = "a worker process without torch (pinned buffers from bcg_host_alloc)"
+        except subprocess.TimeoutExpired:
+            served = {"error": "the served worker ran past 1800 s"}
         except (IndexError, ValueError):
             served = {"error": (sw.stderr or sw.stdout)[-300:]}
 
