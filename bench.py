@@ -377,10 +377,30 @@ def reference_gpu_kernels():
         return {"error": str(e)[:200]}
 
 
+def e2e_in_worker(args, local: int, rank: int, knobs: dict | None) -> dict:
+    """Runs run_e2e_worker in a child process and returns its JSON (or an error)."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--e2e-worker", "--e2e-device", str(local),
+           "--e2e-seed", str(1000 + 97 * rank), "--steps", str(args.steps), "--warmup", str(args.warmup)]
+    if knobs is not None:
+        cmd += ["--e2e-tuning", json.dumps(knobs)]
+    elif args.autotune:
+        cmd.append("--e2e-autotune")
+    try:
+        worker = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+        return json.loads(worker.stdout.strip().splitlines()[-1])
+    except subprocess.TimeoutExpired:
+        return {"error": "the worker ran past 600 s"}
+    except (IndexError, ValueError):
+        return {"error": (worker.stderr or worker.stdout)[-300:]}
+
+
 def run_native(args):
+    world, rank, local = dist_info()
+    # With one GPU the e2e window runs first, before this process loads torch
+    # at all (see the e2e section below); with several, after the ranks meet.
+    early = e2e_in_worker(args, local, rank, None) if world == 1 else None
     import numpy as np
     import torch
-    world, rank, local = dist_info()
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
@@ -478,9 +498,10 @@ def run_native(args):
     plain_ms = s2.elapsed_time(e2) / plain_iters
 
     # ---- end to end through the host API from pinned memory.  The timed window runs in a worker process
-    # that does not load torch (run_e2e_worker): calls from a process that has initialised torch stall now
-    # and then (every ~0.5 s, 7-150 ms), and the same calls from a torch-free process do not.  This process
-    # keeps its own window beside it as `in_process_torch`.
+    # that does not load torch (run_e2e_worker): calls from a process that has loaded torch stall now and
+    # then (every ~0.5 s, 7-150 ms), and the same calls from a torch-free process do not; with one GPU the
+    # worker runs before this process loads torch at all.  This process keeps its own window beside it as
+    # `in_process_torch`.
     a_h = torch.empty((B, N, L), dtype=torch.int32).pin_memory()
     b_h = torch.empty((B, N, L), dtype=torch.int32).pin_memory()
     c_h = torch.empty((B, N, L), dtype=torch.int32).pin_memory()
@@ -492,16 +513,7 @@ def run_native(args):
     knobs = {k: m.get_tuning(k) for k in ("group", "crt_tiles", "crt_persistent", "row_local", "row_rows",
                                            "row_bits", "row_pass", "encode_scalar")}
     barrier()
-    try:
-        worker = subprocess.run([sys.executable, os.path.abspath(__file__), "--e2e-worker", "--e2e-device",
-                                 str(local), "--e2e-seed", str(1000 + 97 * rank), "--e2e-tuning", json.dumps(knobs),
-                                 "--steps", str(args.steps), "--warmup", str(args.warmup)],
-                                capture_output=True, text=True, timeout=600)
-        w = json.loads(worker.stdout.strip().splitlines()[-1])
-    except subprocess.TimeoutExpired:
-        w = {"error": "the worker ran past 600 s"}
-    except (IndexError, ValueError):
-        w = {"error": (worker.stderr or worker.stdout)[-300:]}
+    w = early if early is not None else e2e_in_worker(args, local, rank, knobs)
     barrier()
     with ClockSampler(local) as e2e_clocks:
         t0 = time.perf_counter()
@@ -533,8 +545,9 @@ def run_native(args):
             raise AssertionError("the e2e worker's products differ from the device path's")
         e2e_s = max_over_ranks(w["seconds"])
         e2e_steps, plain_e2e_ms, e2e_clock = w["step_ms"], w["plain_ms_per_product"], w.get("clocks")
-        e2e_where = ("a worker process without torch (pinned buffers from bcg_host_alloc); every distinct "
-                     "product's sha256 equals the device path's")
+        e2e_where = ("a worker process without torch (pinned buffers from bcg_host_alloc)"
+                     + (", run before this process loaded torch" if early is not None else "")
+                     + "; every distinct product's sha256 equals the device path's")
     else:
         e2e_s = max_over_ranks(in_s)
         e2e_steps, plain_e2e_ms, e2e_clock = in_steps, in_plain_ms, in_process["clocks"]
@@ -664,6 +677,8 @@ def run_e2e_worker(args):
     q, a_np, b_np = make_inputs(pkg, args.e2e_seed)
     L = (W + 31) // 32
     m = pkg.Multiplier(N, W, q, device=args.e2e_device)
+    if args.e2e_autotune:
+        m.autotune(max_group=16)
     for k, v in json.loads(args.e2e_tuning or "{}").items():
         m.set_tuning(k, v)
     words = N * L
@@ -1158,6 +1173,7 @@ def main():
     ap.add_argument("--e2e-device", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--e2e-seed", type=int, default=1000, help=argparse.SUPPRESS)
     ap.add_argument("--e2e-tuning", default="", help=argparse.SUPPRESS)
+    ap.add_argument("--e2e-autotune", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.e2e_worker:
         run_e2e_worker(args)
