@@ -137,6 +137,9 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
             bcg::Tuning t = c.tuning();
             t.encode_scalar = uint32_t(value);
             c.set_tuning(t);
+        } else if (k == "host_direct") {
+            require(value == 0 || value == 1, "host_direct must be 0 or 1");
+            c.set_host_direct(value == 1);
         } else if (k == "wait_limit_ns") {
             require(value >= 0 && value <= 60000000000ll, "wait_limit_ns must be in [0, 6e10]");
             c.set_wait_limit_ns(uint64_t(value));
@@ -162,6 +165,7 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         else if (k == "encode_scalar") *value = c.tuning().encode_scalar;
         else if (k == "gap") *value = c.plan().gap;
         else if (k == "wait_limit_ns") *value = int64_t(c.wait_limit_ns());
+        else if (k == "host_direct") *value = c.host_direct() ? 1 : 0;
         else throw std::invalid_argument("unknown tuning knob: " + k);
     });
 }

@@ -626,7 +626,8 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     const uint32_t slots = std::min(kHostSlots, ngroups);
 
     constexpr size_t kPiece = size_t(4) << 20;
-    ensure_host_slots(g, slots, !pageable_direct_ && !(is_pinned(a) && is_pinned(b)), !out_pinned);
+    const bool host_direct = pageable_direct_ && host_direct_;
+    ensure_host_slots(g, slots, !host_direct && !(is_pinned(a) && is_pinned(b)), !out_pinned);
     if (edge_.bytes < 4 * page_size()) edge_.allocate(4 * page_size());
     char* bounce_a = edge_.as<char>();
     char* bounce_b = b != a ? bounce_a + 2 * page_size() : bounce_a;
@@ -643,7 +644,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
             lk.copy_to_device(d, x, gi, bytes, copy_in_, bounce);
             return;
         }
-        if (pageable_direct_) {                // the SMs read it in place, asynchronously
+        if (host_direct) {                     // the SMs read it in place, asynchronously
             check(launch_host_copy(reinterpret_cast<uint32_t*>(d), reinterpret_cast<const uint32_t*>(x), bytes / 4,
                                    copy_in_), "input copy");
             return;
@@ -669,7 +670,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
     // tables (a caller's destination or a pageable output): the SMs write
     // the product there directly, right after the chain; the destination is
     // named while the device computes.
-    const bool direct_out = inline_out && !sink && pageable_direct_;
+    const bool direct_out = inline_out && !sink && host_direct;
     // Larger calls into a pageable output or a caller's destinations lock each
     // group's run of the output as it is issued and copy straight into it.
     const bool run_out = !out_pinned && !inline_out && !sink;
@@ -750,7 +751,7 @@ void Context::multiply_host(const uint32_t* a, const uint32_t* b, uint32_t* c, u
         uint32_t* d = io_dev_[s].as<uint32_t>();
         uint32_t* h = io_in_[s].ptr ? io_in_[s].as<uint32_t>() : nullptr;
         // Packing into the slot's staging: its previous inputs have left for the device.
-        const bool packs = !pageable_direct_ && !(lock_a.engaged() && lock_b_or_a.engaged());
+        const bool packs = !host_direct && !(lock_a.engaged() && lock_b_or_a.engaged());
         if (packs && gi >= slots) check(cudaEventSynchronize(ev_in_[s]), "slot reuse");
         if (gi >= slots) check(cudaStreamWaitEvent(copy_in_, ev_done_[s], 0), "slot reuse");
         // Operand A first: the device encodes it while operand B comes in.

@@ -164,6 +164,10 @@ public:
     // DeviceTimeout; waits on a thread's own copies and MMAs keep kWaitLimitNs.
     void set_wait_limit_ns(uint64_t ns);
     uint64_t wait_limit_ns() const { return enc_.wait_limit_ns; }
+    // Whether host-buffer calls may read and write pageable memory through the
+    // host page tables where the device supports it (default on).
+    void set_host_direct(bool on) { host_direct_ = on; }
+    bool host_direct() const { return host_direct_ && pageable_direct_; }
     // NTT split N = C * 2^row_bits (0: the default R = min(N, 256)); re-plans the NTT tables.
     void set_row_bits(uint32_t row_bits);
 
@@ -195,7 +199,8 @@ private:
     int device_ = 0;
     // The copy engines read pageable host memory through the host page tables
     // (coherent CPU-GPU systems): host inputs then skip the pinned staging copy.
-    bool pageable_direct_ = false;
+    bool pageable_direct_ = false;   // the device reads and writes pageable memory through the host page tables
+    bool host_direct_ = true;        // the host path may use that (knob host_direct)
     cudaStream_t stream_ = nullptr;
     cudaStream_t copy_in_ = nullptr, copy_out_ = nullptr;
     uint32_t group_ = 1;

@@ -104,6 +104,10 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *                native-smoke/rns-encode.cuh:30-77), for L <= 32 only
  *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
  *                Re-plans the twiddle and twist tables (the primes stay).
+ *   "host_direct"  1 (default): where the device reads and writes pageable
+ *                memory through the host's page tables (Grace-based systems),
+ *                small host-buffer calls use copy kernels on it; 0: they pack
+ *                into pinned staging, as on systems without (reads as 0 there)
  *   "wait_limit_ns"  limit of a kernel's wait on another warp role's arrival,
  *                in ns (0: the default, 2 s).  A lower bound: a wait reads the
  *                clock every 64 polls and a poll may sleep up to 20 us, so it

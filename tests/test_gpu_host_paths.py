@@ -218,3 +218,34 @@ def test_host_alloc_buffers():
             pkg.native.host_free(p)
     assert np.array_equal(got, device_products(m, a, b))
     m.close()
+
+
+@pytest.mark.parametrize("N,W,count", [(4096, 868, 5), (65536, 1747, 6)])
+def test_small_calls_without_host_page_tables(N, W, count):
+    """host_direct = 0: small calls pack pageable operands into pinned staging
+    and take outputs back in 4 MiB pieces, the path of systems whose GPU does
+    not use the host page tables; pageable output, sink and named destination
+    all give the device path's products."""
+    pkg = package()
+    q = pkg.inputs.modulus(W, 39)
+    m = pkg.Multiplier(N, W, q)
+    m.set_tuning("host_direct", 0)
+    assert m.get_tuning("host_direct") == 0
+    a, b = operands(pkg, q, N, count, 900)
+    want = device_products(m, a, b)
+    assert np.array_equal(m.multiply(a, b), want)
+    pieces = []
+    m.multiply_sink(a, b, lambda words, n: pieces.append(words.copy()) if words is not None else None)
+    assert np.array_equal(np.concatenate(pieces).reshape(a.shape), want)
+    out = np.zeros(a.size + 3, dtype=np.uint32)[1:1 + a.size]
+    sizes = []
+
+    def dest(n):
+        at = sum(sizes)
+        sizes.append(n)
+        return out.ctypes.data + 4 * at
+
+    m.multiply_dest(a, b, dest)
+    assert np.array_equal(out.reshape(a.shape), want)
+    m.set_tuning("host_direct", 1)
+    m.close()
