@@ -411,7 +411,7 @@ def run_native(args):
     m = pkg.Multiplier(N, W, q, device=local)
     # The autotuner picks this geometry's kernel shapes; the batch's contexts
     # (same geometry) start from its result.
-    tuning = m.autotune(max_group=16) if args.autotune else None
+    tuning = m.autotune(max_group=32) if args.autotune else None
     if args.group:
         m.set_group(args.group)
     group = m.get_tuning("group")
@@ -678,7 +678,7 @@ def run_e2e_worker(args):
     L = (W + 31) // 32
     m = pkg.Multiplier(N, W, q, device=args.e2e_device)
     if args.e2e_autotune:
-        m.autotune(max_group=16)
+        m.autotune(max_group=32)
     for k, v in json.loads(args.e2e_tuning or "{}").items():
         m.set_tuning(k, v)
     words = N * L
@@ -861,7 +861,7 @@ def autotune_geometries(pkg, args, device, geometries):
     out = {}
     for n, w in geometries:
         m = pkg.Multiplier(n, w, pkg.inputs.modulus(w, 1), device=device)
-        r = m.autotune(max_group=16)
+        r = m.autotune(max_group=32)
         out[f"{n}/{w}"] = {k: r[k] for k in ("group", "crt_tiles", "crt_persistent", "row_local", "row_rows", "row_bits",
                                              "row_pass", "us_per_product_tuned")}
         m.close()
