@@ -144,7 +144,7 @@ AutotuneReport autotune(Context& ctx, uint32_t max_group) {
     for (uint32_t rl : {0u, 3u}) { Settings s = cur; s.row_local = rl; consider(s); }
     for (uint32_t rp : {0u, 1u}) { Settings s = cur; s.row_pass = rp; consider(s); }
     for (uint32_t rr : {0u, 8u, 16u, 64u, 128u}) { Settings s = cur; s.row_rows = rr; consider(s); }
-    for (uint32_t gr : {1u, 2u, 4u, 8u, 16u, 32u}) {
+    for (uint32_t gr : {1u, 2u, 4u, 8u, 16u, 32u, 64u}) {
         if (gr > gmax) break;
         Settings s = cur; s.group = gr; consider(s);
     }
