@@ -1110,25 +1110,30 @@ def run_served(pkg, args, device, batched_value, e2e_value=None):
 
 
 def run_profile_case(args):
-    """Small case for ncu: `count` products of N=65536/W=1747 through the device
-    path, once to warm up and `steps` more times (inputs + planes of 2 products
-    exceed L2; a few hundred MB on the device)."""
+    """Small case for ncu: `count` products of N=65536/W=1747 (or --profile-point
+    N,W) through the device path, once to warm up and `steps` more times (inputs
+    + planes of 2 products at N=65536, or 32 at N=16384, exceed L2; a few hundred
+    MB on the device).  --profile-encoder picks the encode kernel."""
     import numpy as np
     import torch
     pkg = importlib.import_module("fherma-bytecrt_gb300")
-    q = pkg.inputs.modulus(W, 2025)
+    n, w = (int(x) for x in args.profile_point.split(",")) if args.profile_point else (N, W)
+    q = pkg.inputs.modulus(w, 2025)
     count = args.profile_count
-    a = np.stack([pkg.inputs.uniform(q, N, 2 * i) for i in range(count)])
-    b = np.stack([pkg.inputs.uniform(q, N, 2 * i + 1) for i in range(count)])
-    m = pkg.Multiplier(N, W, q)
+    a = np.stack([pkg.inputs.uniform(q, n, 2 * i) for i in range(count)])
+    b = np.stack([pkg.inputs.uniform(q, n, 2 * i + 1) for i in range(count)])
+    m = pkg.Multiplier(n, w, q)
     m.set_group(count)
+    if args.profile_encoder == "scalar":
+        m.set_tuning("encode_scalar", 1)
     da = torch.from_numpy(a.view(np.int32)).cuda()
     db = torch.from_numpy(b.view(np.int32)).cuda()
     dc = torch.empty_like(da)
     for _ in range(1 + args.steps):
         m.multiply_device(da, db, dc, count)
     m.synchronize()
-    print(json.dumps({"profile_case": f"{count} products N=65536 W=1747", "launches": m.read_profile()["launches"]}))
+    print(json.dumps({"profile_case": f"{count} products N={n} W={w}, {args.profile_encoder} encoder",
+                      "launches": m.read_profile()["launches"]}))
 
 
 def main():
@@ -1141,6 +1146,9 @@ def main():
                     help="products in the CPU baseline sample, about 10 s on 16 Arm cores (0: skip)")
     ap.add_argument("--profile-case", action="store_true", help="run the small ncu case and exit")
     ap.add_argument("--profile-count", type=int, default=2)
+    ap.add_argument("--profile-point", default="", help="N,W of the profile case (default 65536,1747)")
+    ap.add_argument("--profile-encoder", choices=("tcgen05", "scalar"), default="tcgen05",
+                    help="encode kernel of the profile case")
     ap.add_argument("--group", type=int, default=0, help="products per launch chain (0: library default)")
     ap.add_argument("--profile-every", type=int, default=2,
                     help="time the stages of every k-th launch chain with CUDA events")
