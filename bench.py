@@ -629,7 +629,7 @@ def run_native(args):
         "data": "synthetic (seeded uniform operands in [0,q), seeded odd 1747-bit q; 16 distinct products repeated)",
         "config": {"workload": "batched B=128 exact negacyclic products, N=65536 W=1747 L=55 P=114, one q, "
                                "one CUDA graph per step",
-                   "global_batch": B * world, "per_gpu_batch": B, "group": group, "graph_lanes": args.lanes,
+                   "global_batch": B * world, "per_gpu_batch": B, "group": group, "graph_lanes": args.lanes or "automatic (one branch for one group)",
                    "tuning": {k: m.get_tuning(k) for k in ("crt_tiles", "crt_persistent", "row_local", "row_rows", "row_bits",
                                                            "row_pass")},
                    "autotune": tuning,
@@ -1154,9 +1154,10 @@ def main():
                     help="time the stages of every k-th launch chain with CUDA events")
     ap.add_argument("--no-uneven", dest="uneven", action="store_false", help="skip the uneven 96-product batch")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false", help="keep the default kernel shapes")
-    ap.add_argument("--lanes", type=int, default=1, choices=(1, 2),
-                    help="parallel branches of the timed batch graph that launch chains alternate over (the "
-                         "profiled pass for the rooflines always runs one branch)")
+    ap.add_argument("--lanes", type=int, default=0, choices=(0, 1, 2),
+                    help="parallel branches of the timed batch graphs that launch chains alternate over (0: the "
+                         "library's choice, two for batches of several geometry/modulus groups; the profiled pass "
+                         "for the rooflines always runs one branch)")
     ap.add_argument("--no-served", dest="served", action="store_false", help="skip the served sweep")
     ap.add_argument("--no-encode-kernels", dest="encode_kernels", action="store_false",
                     help="skip comparing the tcgen05 and CUDA-core encoders at small-L points")

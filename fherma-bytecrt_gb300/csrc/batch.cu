@@ -100,7 +100,7 @@ void Batch::add(uint32_t N, uint32_t W, uint32_t L, const uint32_t* q, const uin
 }
 
 void Batch::set_lanes(uint32_t lanes) {
-    if (lanes < 1 || lanes > 2) throw std::invalid_argument("lanes must be 1 or 2");
+    if (lanes > 2) throw std::invalid_argument("lanes must be 0 (automatic), 1 or 2");
     if (lanes == lanes_) return;
     lanes_ = lanes;
     release_graph();
@@ -120,12 +120,13 @@ void Batch::capture() {
             ws_bytes = std::max(ws_bytes, size_t(std::min(e.count, g.ctx->group())) *
                                               g.ctx->workspace_bytes_per_product());
     if (ws_bytes > ws_.bytes) ws_.allocate(ws_bytes);   // release_graph() waited for the last launch
-    if (lanes_ > 1 && ws_bytes > ws2_.bytes) ws2_.allocate(ws_bytes);
+    const uint32_t lanes = this->lanes();
+    if (lanes > 1 && ws_bytes > ws2_.bytes) ws2_.allocate(ws_bytes);
     timer_.reset(profile_every_);
     chains_ = 0;
     check(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal), "graph capture");
     try {
-        if (lanes_ > 1) {   // fork the second branch off the capture stream
+        if (lanes > 1) {   // fork the second branch off the capture stream
             check(cudaEventRecord(fork_, capture_stream_), "graph fork");
             check(cudaStreamWaitEvent(lane_stream_, fork_, 0), "graph fork");
         }
@@ -136,7 +137,7 @@ void Batch::capture() {
             for (const Entry& e : g.entries) {
                 for (uint32_t done = 0; done < e.count; done += chunk) {
                     const uint32_t n = std::min(chunk, e.count - done);
-                    const bool second = lanes_ > 1 && (chains_ & 1);
+                    const bool second = lanes > 1 && (chains_ & 1);
                     timer_.next_chain();
                     ctx.chain(e.a + done * cw, e.b + done * cw, e.c + done * cw, n,
                               (second ? ws2_ : ws_).as<uint32_t>(), second ? lane_stream_ : capture_stream_, &timer_);
@@ -144,7 +145,7 @@ void Batch::capture() {
                 }
             }
         }
-        if (lanes_ > 1) {   // join it back
+        if (lanes > 1) {   // join it back
             check(cudaEventRecord(join_, lane_stream_), "graph join");
             check(cudaStreamWaitEvent(capture_stream_, join_, 0), "graph join");
         }

@@ -266,7 +266,9 @@ int bcg_batch_run(bcg_batch* batch, void* stream);
 int bcg_batch_synchronize(bcg_batch* batch, void* stream);
 int bcg_batch_get_info(bcg_batch* batch, bcg_batch_info* out);   /* captures the graph if needed */
 /* Chains alternate over `lanes` (1 or 2) parallel branches of the graph, each
- * with its own workspace, so that one chain's kernels fill another's tail. */
+ * with its own workspace, so that one chain's kernels fill another's tail.
+ * 0 (the default): two branches when the batch holds several (geometry, q)
+ * groups, one otherwise. */
 int bcg_batch_set_lanes(bcg_batch* batch, uint32_t lanes);
 /* Stage events inside the graph for every k-th chain (recaptures); the
  * profile holds the stage times of the last completed run. */

@@ -44,13 +44,16 @@ def test_uneven_batch_matches_single_products_twice():
         cases.append((N, W, q, a, b, c))
     info = batch.info()
     assert info["groups"] == len(points) and info["products"] == sum(p[3] for p in points)
-    for run in range(2):
+    # Several groups: two graph branches by default; then one, then two again, explicitly.
+    for run, lanes in enumerate((0, 0, 1, 2)):
+        if lanes:
+            batch.set_lanes(lanes)
         for case in cases:
             case[5].fill_(-1)
         batch.run()
         batch.synchronize()
         for N, W, q, a, b, c in cases:
-            assert torch.equal(c, single(pkg, N, W, q, a, b)), (N, W, run)
+            assert torch.equal(c, single(pkg, N, W, q, a, b)), (N, W, run, lanes)
     batch.close()
 
 
