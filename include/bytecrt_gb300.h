@@ -161,11 +161,13 @@ int bcg_multiply(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_
  * the host; `words` is valid only during the call, and the sink must not
  * throw.  The products travel in groups; before the runs of each group the
  * sink is called with words == NULL and n = the group's words: a chance to
- * prepare the destination (the plugin faults in its output pages then).  The
- * sink is called from a library thread, one call at a time, while the calling
- * thread already issues the next groups.  For callers that build their own
- * output container (the plugin's owned std::vector) without filling it first.
- * No counterpart in the reference. */
+ * prepare the destination (fault in or reserve its memory).  The sink is
+ * called one call at a time, in order: from a library thread in calls of three
+ * or more groups (while the calling thread issues the next groups), on the
+ * calling thread in smaller ones.  For callers that append to a container of
+ * their own without filling it first (bcg_multiply_dest below writes into
+ * named memory instead; the plugin shim uses that).  No counterpart in the
+ * reference. */
 typedef void (*bcg_sink)(void* user, const uint32_t* words, size_t n);
 int bcg_multiply_sink(bcg_context* ctx, const uint32_t* a, const uint32_t* b, uint32_t count, bcg_sink sink,
                       void* user);
