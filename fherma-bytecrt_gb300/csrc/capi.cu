@@ -137,6 +137,9 @@ int bcg_context_set_tuning(bcg_context* ctx, const char* knob, int64_t value) {
             bcg::Tuning t = c.tuning();
             t.encode_scalar = uint32_t(value);
             c.set_tuning(t);
+        } else if (k == "host_group") {
+            require(value >= 0 && value <= 4096, "host_group must be in [0, 4096]");
+            c.set_host_group(uint32_t(value));
         } else if (k == "host_direct") {
             require(value == 0 || value == 1, "host_direct must be 0 or 1");
             c.set_host_direct(value == 1);
@@ -166,6 +169,7 @@ int bcg_context_get_tuning(const bcg_context* ctx, const char* knob, int64_t* va
         else if (k == "gap") *value = c.plan().gap;
         else if (k == "wait_limit_ns") *value = int64_t(c.wait_limit_ns());
         else if (k == "host_direct") *value = c.host_direct() ? 1 : 0;
+        else if (k == "host_group") *value = c.host_group();
         else throw std::invalid_argument("unknown tuning knob: " + k);
     });
 }

@@ -178,8 +178,10 @@ uint32_t Context::host_group() const {
     // Host-buffer calls pipeline copies against compute in chunks of about
     // 128 MiB of inputs: the first copy in and the last copy out are not
     // overlapped, and the host link (~200 GB/s each way) makes them cost
-    // more than the slightly shorter launch chains (4 products per chunk at
-    // N = 65536 measured 5.7% faster end to end than 16).
+    // more than the slightly shorter launch chains.  Pinned B = 128 calls at
+    // N = 65536, median per call: 20.48 ms with 4 products per group, 20.55
+    // with 2, 20.90 with 8, 22.04 with 16.
+    if (host_group_) return host_group_;
     const size_t pair_bytes = 2 * coeff_words() * sizeof(uint32_t);
     const uint32_t g = uint32_t(std::max<size_t>(1, (size_t(128) << 20) / pair_bytes));
     return std::min(g, group_);

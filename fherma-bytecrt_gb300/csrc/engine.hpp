@@ -111,6 +111,9 @@ public:
     uint32_t group() const { return group_; }
     // Products per copy/compute chunk of the host-buffer paths.
     uint32_t host_group() const;
+    // Products per host-path group (0: about 128 MiB of operands, at most the chain length).
+    void set_host_group(uint32_t g) { host_group_ = g; }
+    uint32_t host_group_setting() const { return host_group_; }
     void set_group(uint32_t g);
     size_t plane_words() const { return size_t(plan_.g.P) * plan_.g.N; }
     size_t coeff_words() const { return size_t(plan_.g.N) * plan_.g.L; }
@@ -201,6 +204,7 @@ private:
     // (coherent CPU-GPU systems): host inputs then skip the pinned staging copy.
     bool pageable_direct_ = false;   // the device reads and writes pageable memory through the host page tables
     bool host_direct_ = true;        // the host path may use that (knob host_direct)
+    uint32_t host_group_ = 0;        // products per host-path group (knob host_group; 0: automatic)
     cudaStream_t stream_ = nullptr;
     cudaStream_t copy_in_ = nullptr, copy_out_ = nullptr;
     uint32_t group_ = 1;

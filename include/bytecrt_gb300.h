@@ -104,6 +104,10 @@ int bcg_context_set_group(bcg_context* ctx, uint32_t group);
  *                native-smoke/rns-encode.cuh:30-77), for L <= 32 only
  *   "row_bits"   NTT radix split N = C * 2^row_bits (C <= 256); 0: R = min(N, 256).
  *                Re-plans the twiddle and twist tables (the primes stay).
+ *   "host_group"  products per group of a host-buffer call (copies of one
+ *                group overlap the compute of others); 0 (default): about
+ *                128 MiB of operands, at most the chain length.  Reads back the
+ *                value in use
  *   "host_direct"  1 (default): where the device reads and writes pageable
  *                memory through the host's page tables (Grace-based systems),
  *                small host-buffer calls use copy kernels on it; 0: they pack
