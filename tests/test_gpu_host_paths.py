@@ -249,3 +249,23 @@ def test_small_calls_without_host_page_tables(N, W, count):
     assert np.array_equal(out.reshape(a.shape), want)
     m.set_tuning("host_direct", 1)
     m.close()
+
+
+@pytest.mark.parametrize("host_group", [1, 2, 3, 8])
+def test_host_group_knob(host_group):
+    """Any number of products per host-path group gives the device path's products (pageable and pinned)."""
+    pkg = package()
+    N, W, count = 65536, 1747, 9
+    q = pkg.inputs.modulus(W, 40)
+    m = pkg.Multiplier(N, W, q)
+    m.set_tuning("host_group", host_group)
+    assert m.get_tuning("host_group") == host_group
+    a, b = operands(pkg, q, N, count, 1000)
+    want = device_products(m, a, b)
+    assert np.array_equal(m.multiply(a, b), want)
+    ta = torch.from_numpy(a.view(np.int32)).pin_memory()
+    tb = torch.from_numpy(b.view(np.int32)).pin_memory()
+    tc = torch.zeros_like(ta).pin_memory()
+    m.multiply_into(ta, tb, tc, count)
+    assert np.array_equal(tc.numpy().view(np.uint32), want)
+    m.close()
