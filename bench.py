@@ -643,8 +643,9 @@ def run_native(args):
                             "max": max(e2e_steps), "each": [round(t, 2) for t in e2e_steps]},
                 "clocks": e2e_clock, "measured_in": e2e_where, "in_process_torch": in_process,
                 "median_call_products_per_s": world * B / (sorted(e2e_steps)[len(e2e_steps) // 2] / 1000.0),
-                "median_call_note": "B / the median call's time: the rate without the box's occasional stalled "
-                                    "calls; `value` above is the whole window, stalls included",
+                "median_call_note": "B / the median call's time: the rate without the calls that stall on the "
+                                    "device's page faults on the host buffers (their number grows over a box's "
+                                    "life); `value` above is the whole window, stalls included",
                 "host_link": link},
         "stream_launch": {"products_per_s": stream_value, "ms_per_step": stream_ms / max(3, args.steps // 2)},
         "plain": {"device_ms_per_product": plain_ms, "device_products_per_s": 1000.0 / plain_ms,
